@@ -1,0 +1,204 @@
+// common.cuh -- complex arithmetic and in-register DFT codelets for the
+// sm_103a transform kernels.
+//
+// Conventions (same as the reference genFFT, fft.h:80-85, FFTTwiddle.h:44-51):
+//   forward  X[k] = sum_n x[n] * exp(-2*pi*i*n*k/N)
+//   inverse  x[n] = sum_k X[k] * exp(+2*pi*i*n*k/N)   (unscaled)
+// Complex values are interleaved {re, im} pairs (float2 / double2 layout).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <type_traits>
+
+namespace gfft {
+
+template <typename T>
+struct alignas(2 * sizeof(T)) cpx {
+    T x, y;
+};
+
+template <typename T>
+__device__ __forceinline__ cpx<T> mk(T a, T b) { return cpx<T>{a, b}; }
+template <typename T>
+__device__ __forceinline__ cpx<T> operator+(cpx<T> a, cpx<T> b) { return {a.x + b.x, a.y + b.y}; }
+template <typename T>
+__device__ __forceinline__ cpx<T> operator-(cpx<T> a, cpx<T> b) { return {a.x - b.x, a.y - b.y}; }
+template <typename T>
+__device__ __forceinline__ cpx<T> operator-(cpx<T> a) { return {-a.x, -a.y}; }
+
+// complex product a*b
+template <typename T>
+__device__ __forceinline__ cpx<T> cmul(cpx<T> a, cpx<T> b)
+{
+    return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
+}
+// a * conj(b)
+template <typename T>
+__device__ __forceinline__ cpx<T> cmulc(cpx<T> a, cpx<T> b)
+{
+    return {a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y};
+}
+// twiddle product in the transform's direction: forward multiplies by w,
+// inverse by conj(w) (tables hold the forward twiddles exp(-2 pi i k/N)).
+template <bool INV, typename T>
+__device__ __forceinline__ cpx<T> twmul(cpx<T> a, cpx<T> w)
+{
+    return INV ? cmulc(a, w) : cmul(a, w);
+}
+template <typename T>
+__device__ __forceinline__ cpx<T> conj(cpx<T> a) { return {a.x, -a.y}; }
+
+__host__ __device__ constexpr int ipow(int b, int e) { return e <= 0 ? 1 : b * ipow(b, e - 1); }
+
+// vector loads/stores of one complex value (8 or 16 bytes, naturally aligned)
+template <typename T>
+struct vec2;
+template <>
+struct vec2<float> { using type = float2; };
+template <>
+struct vec2<double> { using type = double2; };
+
+// read-only path (twiddle tables)
+template <typename T>
+__device__ __forceinline__ cpx<T> ldg_c(const cpx<T> *p)
+{
+    auto v = __ldg(reinterpret_cast<const typename vec2<T>::type *>(p));
+    return {v.x, v.y};
+}
+// plain global load
+template <typename T>
+__device__ __forceinline__ cpx<T> ld_c(const cpx<T> *p)
+{
+    auto v = *reinterpret_cast<const typename vec2<T>::type *>(p);
+    return {v.x, v.y};
+}
+// streaming (evict-first) global load / store for data touched once
+template <typename T>
+__device__ __forceinline__ cpx<T> ldcs_c(const cpx<T> *p)
+{
+    auto v = __ldcs(reinterpret_cast<const typename vec2<T>::type *>(p));
+    return {v.x, v.y};
+}
+template <typename T>
+__device__ __forceinline__ void stcs_c(cpx<T> *p, cpx<T> a)
+{
+    typename vec2<T>::type v;
+    v.x = a.x;
+    v.y = a.y;
+    __stcs(reinterpret_cast<typename vec2<T>::type *>(p), v);
+}
+template <typename T>
+__device__ __forceinline__ void st_c(cpx<T> *p, cpx<T> a)
+{
+    typename vec2<T>::type v;
+    v.x = a.x;
+    v.y = a.y;
+    *reinterpret_cast<typename vec2<T>::type *>(p) = v;
+}
+
+// ---------------------------------------------------------------------------
+// Multiplication by the compile-time root W_16^k = exp(-2 pi i k / 16)
+// (forward) or its conjugate (inverse).  Trivial roots cost no multiply,
+// the 45-degree roots two.  Constants are the correctly rounded values of
+// cos(pi/8), sin(pi/8) and sqrt(1/2).
+template <typename T>
+struct K16 {
+    static constexpr double C1 = 0.92387953251128675613;  // cos(pi/8)
+    static constexpr double S1 = 0.38268343236508977173;  // sin(pi/8)
+    static constexpr double R2 = 0.70710678118654752440;  // sqrt(1/2)
+};
+
+// cos(2 pi k / 16) for k in [0, 16)
+template <typename T>
+__host__ __device__ constexpr T cos16(int k)
+{
+    return k == 0 ? (T)1 : k == 1 ? (T)K16<T>::C1 : k == 2 ? (T)K16<T>::R2 : k == 3 ? (T)K16<T>::S1
+         : k == 4 ? (T)0 : k == 5 ? -(T)K16<T>::S1 : k == 6 ? -(T)K16<T>::R2 : k == 7 ? -(T)K16<T>::C1
+         : k == 8 ? (T)-1 : k == 9 ? -(T)K16<T>::C1 : k == 10 ? -(T)K16<T>::R2 : k == 11 ? -(T)K16<T>::S1
+         : k == 12 ? (T)0 : k == 13 ? (T)K16<T>::S1 : k == 14 ? (T)K16<T>::R2 : (T)K16<T>::C1;
+}
+
+// compile-time loop: f(std::integral_constant<int, I>) for I in [B, E)
+template <int B, int E, typename F>
+__device__ __forceinline__ void static_for(F &&f)
+{
+    if constexpr (B < E) {
+        f(std::integral_constant<int, B>{});
+        static_for<B + 1, E>(f);
+    }
+}
+
+template <int K, bool INV, typename T>
+__device__ __forceinline__ cpx<T> rot16(cpx<T> a)
+{
+    // exponent of the effective forward root after folding direction
+    constexpr int k = INV ? ((16 - (K % 16)) % 16) : (K % 16);
+    constexpr T r2 = (T)K16<T>::R2;
+    if constexpr (k == 0) return a;
+    else if constexpr (k == 4) return {a.y, -a.x};     // * (-i)
+    else if constexpr (k == 8) return {-a.x, -a.y};    // * (-1)
+    else if constexpr (k == 12) return {-a.y, a.x};    // * (+i)
+    else if constexpr (k == 2) return {r2 * (a.x + a.y), r2 * (a.y - a.x)};      // (r2, -r2)
+    else if constexpr (k == 6) return {r2 * (a.y - a.x), -r2 * (a.x + a.y)};     // (-r2, -r2)
+    else if constexpr (k == 10) return {-r2 * (a.x + a.y), r2 * (a.x - a.y)};    // (-r2, r2)
+    else if constexpr (k == 14) return {r2 * (a.x - a.y), r2 * (a.x + a.y)};     // (r2, r2)
+    else {
+        // general root: cos(2 pi k/16), -sin(2 pi k/16)
+        constexpr T wr = cos16<T>(k);
+        constexpr T wi = -cos16<T>((k + 12) % 16);  // sin(t) = cos(t - pi/2)
+        return {a.x * wr - a.y * wi, a.x * wi + a.y * wr};
+    }
+}
+
+// ---------------------------------------------------------------------------
+// In-register DFT of R points (R = 1, 2, 4, 8, 16), natural order in and
+// out, stride-1 over the array v.  R = 8 and 16 are split as A x B
+// (A = 2 or 4): n = n1 + A*n2, k = k1 + B*k2,
+//   X[k1 + B k2] = sum_n1 W_A^(n1 k2) W_R^(n1 k1) sum_n2 x[n1 + A n2] W_B^(n2 k1)
+template <int R, bool INV, typename T>
+__device__ __forceinline__ void dft(cpx<T> *v)
+{
+    if constexpr (R == 1) {
+        return;
+    } else if constexpr (R == 2) {
+        cpx<T> a = v[0], b = v[1];
+        v[0] = a + b;
+        v[1] = a - b;
+    } else if constexpr (R == 4) {
+        cpx<T> s02 = v[0] + v[2], d02 = v[0] - v[2];
+        cpx<T> s13 = v[1] + v[3], d13 = v[1] - v[3];
+        // forward: X1 = d02 - i d13, X3 = d02 + i d13
+        cpx<T> jd13 = INV ? cpx<T>{-d13.y, d13.x} : cpx<T>{d13.y, -d13.x};  // (-+i) * d13
+        v[0] = s02 + s13;
+        v[2] = s02 - s13;
+        v[1] = d02 + jd13;
+        v[3] = d02 - jd13;
+    } else {
+        constexpr int A = (R == 16) ? 4 : 2;
+        constexpr int B = R / A;
+        cpx<T> y[A][B];
+#pragma unroll
+        for (int n1 = 0; n1 < A; n1++) {
+#pragma unroll
+            for (int n2 = 0; n2 < B; n2++) y[n1][n2] = v[n1 + A * n2];
+            dft<B, INV, T>(y[n1]);
+        }
+        // inner twiddles W_R^(n1 k1) = W_16^(n1 k1 16/R)
+        constexpr int S = 16 / R;
+        static_for<0, B>([&](auto k1c) {
+            constexpr int k1 = decltype(k1c)::value;
+            cpx<T> z[A];
+            static_for<0, A>([&](auto n1c) {
+                constexpr int n1 = decltype(n1c)::value;
+                z[n1] = rot16<n1 * k1 * S, INV, T>(y[n1][k1]);
+            });
+            dft<A, INV, T>(z);
+#pragma unroll
+            for (int k2 = 0; k2 < A; k2++) v[k1 + B * k2] = z[k2];
+        });
+    }
+}
+
+}  // namespace gfft

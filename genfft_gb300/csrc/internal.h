@@ -1,0 +1,43 @@
+// internal.h -- declarations shared by the host planner (api.cpp) and the
+// kernel translation units.  Not part of the public ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <string>
+
+#include "../../include/genfft_gb300.h"
+
+namespace gfft {
+
+// thrown inside the library, converted to a status at the C boundary
+struct Error {
+    gfft_status status;
+    std::string msg;
+};
+[[noreturn]] void fail(gfft_status st, const std::string &msg);
+void check_cuda(cudaError_t e, const char *what);
+
+// ---- fused single-kernel C2C (c2c_fused.cu) ------------------------------
+struct FusedC2CArgs {
+    const void *in;
+    void *out;
+    long long batch;
+    long long idist, odist;       // elements between transforms
+    long long istride, ostride;   // elements between points
+    const void *tw;               // device twiddle table for (dtype, logn)
+};
+int fused_max_logn(int dtype);
+size_t fused_twiddle_count(int dtype, int logn);              // complex elements
+void fused_twiddle_fill(int dtype, int logn, void *host_buf);  // writes that many
+cudaError_t launch_fused_c2c(int dtype, int logn, int inverse, const FusedC2CArgs &a,
+                             cudaStream_t st);
+
+// ---- device twiddle cache (api.cpp) --------------------------------------
+// Returns a device pointer to the table made by `fill` (count complex
+// elements of dtype), cached per (device, key) for the process lifetime.
+const void *cached_table(const std::string &key, int dtype, size_t count,
+                         void (*fill)(int, int, void *), int logn);
+
+}  // namespace gfft

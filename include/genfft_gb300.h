@@ -1,0 +1,119 @@
+/*
+ * genfft_gb300.h -- C ABI of libgenfft_gb300.so, the GB300 (sm_103a)
+ * implementation of genFFT's transform hot path.
+ *
+ * Plain C: pointers, sizes and status codes only.  Data pointers passed to
+ * the gfft_* transform entry points are DEVICE pointers (cudaMalloc'd or
+ * managed) unless the function name ends in _host; `stream` is a
+ * cudaStream_t passed as void* (NULL = the legacy default stream).  Calls are
+ * stream-ordered and return as soon as the work is enqueued.
+ *
+ * Conventions follow the reference library (mzient/genFFT):
+ *   - power-of-two sizes only (README.txt:10-11);
+ *   - forward transform uses exp(-2*pi*i*j*k/n) (FFTTwiddle.h:44-51);
+ *   - the inverse is UNSCALED: inverse(forward(x)) == n * x (README.txt:28-31);
+ *   - complex data is interleaved {re, im} pairs of float or double
+ *     (FFTComplex.h:33-37);
+ *   - row strides are in complex elements for complex arrays and in scalar
+ *     elements for real arrays (fft.h:140-146, FFTReal.h:330-335).
+ * Where the reference asserts or has undefined behaviour (unsupported sizes,
+ * fft_impl_generic.h:276-278), these functions return an error status and
+ * record a message readable with gfft_last_error().
+ */
+#ifndef GENFFT_GB300_H
+#define GENFFT_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GFFT_VERSION 1
+
+typedef enum gfft_status {
+    GFFT_OK = 0,
+    GFFT_ERR_INVALID_SIZE = 1,   /* not a power of two, zero/negative, or above the limit */
+    GFFT_ERR_INVALID_VALUE = 2,  /* bad enum, NULL pointer, bad stride */
+    GFFT_ERR_ALIAS = 3,          /* out == in where the reference forbids it */
+    GFFT_ERR_ALIGN = 4,          /* pointer not aligned to its element type */
+    GFFT_ERR_ARCH = 5,           /* no sm_103 device current */
+    GFFT_ERR_CUDA = 6,           /* a CUDA runtime call failed */
+    GFFT_ERR_TIMEOUT = 7,        /* a bounded device-side wait gave up */
+    GFFT_ERR_UNSUPPORTED = 8,    /* valid request this build does not implement */
+    GFFT_ERR_ALLOC = 9,          /* device or host allocation failed */
+    GFFT_ERR_INVALID_PLAN = 10   /* NULL or destroyed plan handle */
+} gfft_status;
+
+typedef enum gfft_dtype { GFFT_F32 = 0, GFFT_F64 = 1 } gfft_dtype;
+
+typedef enum gfft_kind {
+    GFFT_KIND_C2C = 0,     /* batched 1D complex, FFT<T> (fft.h:56-113) */
+    GFFT_KIND_R2C = 1,     /* batched 1D real input, RealFFT<T> (FFTReal.h:186-221) */
+    GFFT_KIND_C2C_2D = 2,  /* 2D complex, FFT2D<T> (fft.h:198-245) */
+    GFFT_KIND_R2C_2D = 3,  /* 2D real input, RealFFT2D<T> (FFTReal.h:69-184) */
+    GFFT_KIND_VERT = 4     /* column FFT, FFTVert<T> (fft.h:115-171) */
+} gfft_kind;
+
+typedef enum gfft_mode {
+    GFFT_MODE_PLAIN = 0    /* FP32/FP64 CUDA-core arithmetic */
+} gfft_mode;
+
+/* gfft_desc.flags */
+#define GFFT_FLAG_HALF_SPECTRUM 0x1u /* R2C: store n/2+1 bins (RealFFT::forward half=true) */
+#define GFFT_FLAG_BITREV_INPUT 0x2u  /* C2C/VERT: input in bit-reversed order
+                                        (transform_no_scramble, fft.h:69-73, 132-136) */
+
+typedef struct gfft_desc {
+    int kind;             /* gfft_kind */
+    int dtype;            /* gfft_dtype */
+    int mode;             /* gfft_mode */
+    unsigned flags;       /* GFFT_FLAG_* */
+    long long n0;         /* 1D/VERT: transform length; 2D: width (columns) */
+    long long n1;         /* 2D: height (rows); VERT: number of columns; else 0 */
+    long long batch;      /* number of transforms (>= 1) */
+    long long istride;    /* input element stride (0 = contiguous = 1); VERT: row stride */
+    long long idist;      /* input distance between transforms (0 = dense) */
+    long long ostride;    /* output element stride (0 = 1); VERT: row stride */
+    long long odist;      /* output distance between transforms (0 = dense) */
+} gfft_desc;
+
+typedef struct gfft_plan_s *gfft_plan;
+
+/* ---- plan API -------------------------------------------------------- */
+/* Plans are immutable after creation and may be executed concurrently on
+ * different streams; each exec uses its own slice of nothing but the plan's
+ * read-only tables.  Creation is thread-safe. */
+gfft_status gfft_plan_create(gfft_plan *plan, const gfft_desc *desc);
+gfft_status gfft_plan_destroy(gfft_plan plan);
+/* forward (inverse = 0) or unscaled inverse (inverse = 1) on device memory */
+gfft_status gfft_exec(gfft_plan plan, int inverse, void *out, const void *in, void *stream);
+/* Same transform on HOST buffers (the reference's calling convention):
+ * copies in, transforms and copies out in pipelined chunks, synchronously.
+ * Pinned host memory gives full link bandwidth; pageable memory works. */
+gfft_status gfft_exec_host(gfft_plan plan, int inverse, void *out, const void *in);
+/* number of kernel launches one gfft_exec makes (for launch accounting) */
+gfft_status gfft_plan_launches(gfft_plan plan, int *launches);
+
+/* ---- reference-shaped entry points (device pointers) ------------------ */
+/* Each mirrors one call of the reference C++ API; plans are cached per
+ * (kind, type, size) like the reference's per-size singletons
+ * (FFTLevel.h:76-88), but creation here is mutex-guarded. */
+
+/* FFT<T>(n).transform<inverse>(out, in) over `batch` dense transforms
+ * (fft.h:80-85).  out != in is not required here (in-place is allowed). */
+gfft_status gfft_fft_transform(int dtype, int n, long long batch, int inverse, void *out,
+                               const void *in, void *stream);
+
+const char *gfft_status_string(gfft_status status);
+/* message of the last failed call on this thread ("" if none) */
+const char *gfft_last_error(void);
+int gfft_version(void);
+/* largest n handled by a single fused kernel for dtype (informational) */
+int gfft_max_fused_size(int dtype);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GENFFT_GB300_H */
