@@ -38,6 +38,8 @@ WORKLOADS = {
     "c2c_f32_4096x16384": ("c2c", "f32", 1 << 12, 0, 16384),
     "c2c_f32_1024x65536": ("c2c", "f32", 1 << 10, 0, 65536),
     "c2c_f64_4096x8192": ("c2c", "f64", 1 << 12, 0, 8192),
+    "c2c_f32_4194304x32": ("c2c", "f32", 1 << 22, 0, 32),
+    "c2c_f64_65536x512": ("c2c", "f64", 1 << 16, 0, 512),
 }
 DEFAULT = "c2c_f32_4096x16384"
 
@@ -87,12 +89,59 @@ def traffic_from_profile(workload):
 
 
 class ClockSampler:
+    """Samples SM clock, power and clock-event reasons during the timed
+    region: NVML through ctypes every 2 ms (a thread), else nvidia-smi."""
+
     def __init__(self, device):
         self.device = device
+        self.rows = []
+        self._stop = None
+        self._thr = None
         self.proc = None
 
+    def _nvml_index(self):
+        vis = os.environ.get("CUDA_VISIBLE_DEVICES", "")
+        ids = [v.strip() for v in vis.split(",") if v.strip()]
+        if ids and ids[0].isdigit() and self.device < len(ids):
+            return int(ids[self.device])
+        return self.device
+
+    def _start_nvml(self):
+        import threading
+        try:
+            nv = ctypes.CDLL("libnvidia-ml.so.1")
+        except OSError:
+            return False
+        if nv.nvmlInit_v2() != 0:
+            return False
+        h = ctypes.c_void_p()
+        if nv.nvmlDeviceGetHandleByIndex_v2(self._nvml_index(), ctypes.byref(h)) != 0:
+            return False
+        get_reasons = getattr(nv, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            getattr(nv, "nvmlDeviceGetCurrentClocksThrottleReasons")
+        mx = ctypes.c_uint()
+        nv.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx))
+        self._max = float(mx.value)
+        self._stop = threading.Event()
+
+        def loop():
+            clk, pw, rs = ctypes.c_uint(), ctypes.c_uint(), ctypes.c_ulonglong()
+            while not self._stop.is_set():
+                nv.nvmlDeviceGetClockInfo(h, 1, ctypes.byref(clk))
+                nv.nvmlDeviceGetPowerUsage(h, ctypes.byref(pw))
+                get_reasons(h, ctypes.byref(rs))
+                self.rows.append((float(clk.value), self._max, pw.value / 1000.0, int(rs.value)))
+                time.sleep(0.002)
+
+        self._thr = threading.Thread(target=loop, daemon=True)
+        self._thr.start()
+        time.sleep(0.01)
+        return True
+
     def __enter__(self):
-        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active")
+        if self._start_nvml():
+            return self
+        q = "clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active"
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.device}", f"--query-gpu={q}", "--format=csv,noheader,nounits",
@@ -102,7 +151,10 @@ class ClockSampler:
         return self
 
     def __exit__(self, *exc):
-        self.rows = []
+        if self._thr is not None:
+            self._stop.set()
+            self._thr.join()
+            return
         if self.proc is None:
             return
         self.proc.terminate()
@@ -121,7 +173,7 @@ class ClockSampler:
                 continue
 
     def summary(self):
-        rows = getattr(self, "rows", [])
+        rows = self.rows
         if not rows:
             return None
         busy = [r for r in rows if not (r[3] & 0x1)] or rows
@@ -131,7 +183,8 @@ class ClockSampler:
                 if r[3] & bit and bit != 0x1:
                     reasons.add(name)
         return {"sm_mhz": statistics.median(r[0] for r in busy), "sm_max_mhz": max(r[1] for r in rows),
-                "power_w_max": max(r[2] for r in rows), "samples": len(rows), "reasons": sorted(reasons)}
+                "power_w_max": max(r[2] for r in rows), "samples": len(rows),
+                "source": "nvml" if self._thr is not None else "nvidia-smi", "reasons": sorted(reasons)}
 
 
 # ---------------------------------------------------------------------------
@@ -354,7 +407,7 @@ def run_ours(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT)

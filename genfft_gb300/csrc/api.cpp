@@ -11,7 +11,9 @@
 
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <algorithm>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -20,14 +22,29 @@
 #include <vector>
 
 #include "internal.h"
+#include "tiles_registry.h"
+#include "twiddle.h"
+
+enum { ALGO_NONE = 0, ALGO_FUSED = 1, ALGO_FOURSTEP = 2 };
 
 struct gfft_plan_s {
     gfft_desc d;
     int device = 0;
     int logn0 = 0, logn1 = 0;
-    int algo = 0;             // 1 = fused single-kernel C2C
-    const void *tw = nullptr; // device twiddle table (cached, not owned)
+    int algo = ALGO_NONE;
+    const void *tw = nullptr; // fused: device twiddle table (cached, not owned)
     int launches = 0;
+    // four-step (N = A * B): column pass over B columns of A points, row
+    // pass over A rows of B points; `group` transforms per launch pair so
+    // the intermediate (group * N elements) stays in L2
+    int logA = 0, logB = 0;
+    const gfft::TileKernel *kcol = nullptr, *krow = nullptr;
+    int ccol = 0, crow = 0;
+    const void *tw_col = nullptr, *tw_row = nullptr, *tw_lo = nullptr, *tw_hi = nullptr;
+    int lo_bits = 0;
+    long long group = 0;
+    void *ws = nullptr;
+    size_t ws_bytes = 0;
     unsigned magic = 0x6766u;
     // host-path staging (owned, lazily allocated)
     std::mutex host_mu;
@@ -80,7 +97,7 @@ static void check_device()
 }
 
 const void *cached_table(const std::string &key, int dtype, size_t count,
-                         void (*fill)(int, int, void *), int logn)
+                         const std::function<void(void *)> &fill)
 {
     static std::mutex mu;
     static std::map<std::pair<int, std::string>, void *> cache;
@@ -92,7 +109,7 @@ const void *cached_table(const std::string &key, int dtype, size_t count,
     if (it != cache.end()) return it->second;
     const size_t bytes = std::max<size_t>(count, 1) * cplx_bytes(dtype);
     std::vector<unsigned char> host(bytes, 0);
-    if (count) fill(dtype, logn, host.data());
+    if (count) fill(host.data());
     void *d = nullptr;
     check_cuda(cudaMalloc(&d, bytes), "cudaMalloc(twiddles)");
     cudaError_t e = cudaMemcpy(d, host.data(), bytes, cudaMemcpyHostToDevice);
@@ -119,19 +136,88 @@ static void validate_desc(const gfft_desc &d)
         fail(GFFT_ERR_INVALID_VALUE, "unknown flag bits");
 }
 
+static const void *tile_table(int dtype, const TileKernel *k, int logl, int c)
+{
+    return cached_table("tile/" + std::to_string(dtype) + "/" + std::to_string(logl) + "/" + std::to_string(c) +
+                            "/" + std::to_string(k->threads),
+                        dtype, k->twcount, [k](void *buf) { k->fill(buf); });
+}
+
+// W_N^e split as tw_hi[e >> lo_bits] * tw_lo[e & (2^lo_bits - 1)]
+static void four_step_tables(gfft_plan_s &p, int logn)
+{
+    const int dtype = p.d.dtype;
+    const int lo_bits = (logn + 1) / 2;
+    const long long N = 1LL << logn;
+    p.lo_bits = lo_bits;
+    auto fill = [dtype, N](long long count, long long mul) {
+        return [dtype, N, count, mul](void *buf) {
+            for (long long e = 0; e < count; e++) {
+                if (dtype == GFFT_F32) {
+                    float *o = static_cast<float *>(buf);
+                    forward_root<float>(e * mul, N, &o[2 * e], &o[2 * e + 1]);
+                } else {
+                    double *o = static_cast<double *>(buf);
+                    forward_root<double>(e * mul, N, &o[2 * e], &o[2 * e + 1]);
+                }
+            }
+        };
+    };
+    const std::string key = "4s/" + std::to_string(dtype) + "/" + std::to_string(logn);
+    p.tw_lo = cached_table(key + "/lo", dtype, 1LL << lo_bits, fill(1LL << lo_bits, 1));
+    p.tw_hi = cached_table(key + "/hi", dtype, N >> lo_bits, fill(N >> lo_bits, 1LL << lo_bits));
+}
+
+static long long env_ll(const char *name, long long dflt)
+{
+    const char *v = std::getenv(name);
+    return (v && *v) ? std::atoll(v) : dflt;
+}
+
+static void plan_fourstep(gfft_plan_s &p, int logn)
+{
+    const gfft_desc &d = p.d;
+    if (d.istride != 1 || d.ostride != 1)
+        fail(GFFT_ERR_UNSUPPORTED, "sizes above the fused limit need unit element strides");
+    if (logn > 24) fail(GFFT_ERR_INVALID_SIZE, "size above 2^24 is not supported");
+    // A (column-FFT length) and B (row-FFT length), both at most 2^12
+    p.logA = logn / 2;
+    p.logB = logn - p.logA;
+    const long long maxc = env_ll("GFFT_TILE_MAXC", 16);
+    p.ccol = tile_widest(d.dtype, TILE_COL_TW4, p.logA, (int)maxc);
+    p.crow = tile_widest(d.dtype, TILE_ROW_XPOSE, p.logB, (int)maxc);
+    if (!p.ccol || !p.crow) fail(GFFT_ERR_UNSUPPORTED, "no tile kernel for this size");
+    p.kcol = tile_find(d.dtype, TILE_COL_TW4, p.logA, p.ccol);
+    p.krow = tile_find(d.dtype, TILE_ROW_XPOSE, p.logB, p.crow);
+    p.tw_col = tile_table(d.dtype, p.kcol, p.logA, p.ccol);
+    p.tw_row = tile_table(d.dtype, p.krow, p.logB, p.crow);
+    four_step_tables(p, logn);
+    // group so the intermediate fits comfortably in the 129 MB L2
+    const long long N = 1LL << logn;
+    const long long l2_budget = env_ll("GFFT_L2_BUDGET_MB", 48) << 20;
+    p.group = std::max<long long>(1, l2_budget / (N * (long long)cplx_bytes(d.dtype)));
+    p.group = std::min(p.group, std::max<long long>(1, d.batch));
+    p.ws_bytes = (size_t)(p.group * N) * cplx_bytes(d.dtype);
+    check_cuda(cudaMalloc(&p.ws, p.ws_bytes), "cudaMalloc(workspace)");
+    p.algo = ALGO_FOURSTEP;
+    p.launches = 2 * (int)((d.batch + p.group - 1) / p.group);
+}
+
 static void plan_c2c(gfft_plan_s &p)
 {
     const gfft_desc &d = p.d;
     if (d.flags & GFFT_FLAG_BITREV_INPUT) fail(GFFT_ERR_UNSUPPORTED, "bit-reversed input not built yet");
     p.logn0 = ilog2ll(d.n0);
     if (p.logn0 <= fused_max_logn(d.dtype)) {
-        p.algo = 1;
+        const int logn = p.logn0, dtype = d.dtype;
+        p.algo = ALGO_FUSED;
         p.launches = 1;
-        p.tw = cached_table("fused/" + std::to_string(d.dtype) + "/" + std::to_string(p.logn0), d.dtype,
-                            fused_twiddle_count(d.dtype, p.logn0), &fused_twiddle_fill, p.logn0);
+        p.tw = cached_table("fused/" + std::to_string(dtype) + "/" + std::to_string(logn), dtype,
+                            fused_twiddle_count(dtype, logn),
+                            [dtype, logn](void *buf) { fused_twiddle_fill(dtype, logn, buf); });
         return;
     }
-    fail(GFFT_ERR_UNSUPPORTED, "C2C size above the fused limit is not built yet");
+    plan_fourstep(p, p.logn0);
 }
 
 static gfft_plan_s *make_plan(const gfft_desc &in)
@@ -171,9 +257,28 @@ static void exec_plan(gfft_plan_s &p, int inverse, void *out, const void *in, cu
     check_ptr(out, d.dtype, "out");
     const long long batch = batch_override >= 0 ? batch_override : d.batch;
     switch (p.algo) {
-    case 1: {
+    case ALGO_FUSED: {
         FusedC2CArgs a{in, out, batch, d.idist, d.odist, d.istride, d.ostride, p.tw};
         check_cuda(launch_fused_c2c(d.dtype, p.logn0, inverse, a, st), "launch fused C2C");
+        break;
+    }
+    case ALGO_FOURSTEP: {
+        const long long A = 1LL << p.logA, B = 1LL << p.logB, N = A * B;
+        const size_t eb = cplx_bytes(d.dtype);
+        const unsigned nmask = (unsigned)(N - 1);
+        for (long long g0 = 0; g0 < batch; g0 += p.group) {
+            const long long nb = std::min(p.group, batch - g0);
+            const char *src = static_cast<const char *>(in) + (size_t)(g0 * d.idist) * eb;
+            char *dst = static_cast<char *>(out) + (size_t)(g0 * d.odist) * eb;
+            // column pass: B columns of A points, stride B, into the workspace
+            check_cuda(launch_colpass(*p.kcol, inverse, B / p.ccol, nb, src, p.ws, B, B, B, d.idist, N,
+                                      p.tw_col, p.tw_lo, p.tw_hi, p.lo_bits, nmask, st),
+                       "launch column pass");
+            // row pass: A rows of B points, stored transposed (stride A)
+            check_cuda(launch_rowpass(*p.krow, inverse, A / p.crow, nb, p.ws, dst, A, B, A, N, d.odist,
+                                      p.tw_row, st),
+                       "launch row pass");
+        }
         break;
     }
     default:
@@ -250,7 +355,7 @@ static gfft_plan_s *cached_plan(int kind, int dtype, long long n0, long long n1,
     d.flags = flags;
     d.n0 = n0;
     d.n1 = n1;
-    d.batch = 1;
+    d.batch = 1 << 20;  // sizes the workspace for full groups; the batch is per call
     gfft_plan_s *p = make_plan(d);
     cache.emplace(key, p);
     return p;
@@ -301,6 +406,7 @@ gfft_status gfft_plan_destroy(gfft_plan plan)
             if (p->stage_out[i]) cudaFree(p->stage_out[i]);
             if (p->host_streams[i]) cudaStreamDestroy(p->host_streams[i]);
         }
+        if (p->ws) cudaFree(p->ws);
         p->magic = 0;
         delete p;
     });

@@ -64,8 +64,9 @@ __global__ void __launch_bounds__(FusedCfg<T, LOGN>::THREADS)
 #pragma unroll
         for (int q = 0; q < E; q++) v[q] = cpx<T>{(T)0, (T)0};
     }
-    stockham_run<T, LOGN, FusedE<T>::value, INV>(v, t, sm + g * SP::SMEM, tw,
-                                                  []() { __syncthreads(); });
+    cpx<T> *my = sm + g * SP::SMEM;
+    stockham_run<T, LOGN, FusedE<T>::value, INV>(
+        v, t, [my](int i) -> cpx<T> & { return my[spad<T>(i)]; }, tw, []() { __syncthreads(); });
     if (active) {
         cpx<T> *dst = out + b * odist + (long long)t * ostride;
 #pragma unroll
@@ -81,17 +82,8 @@ namespace {
 template <typename T, int LOGN>
 void fill_tw(void *buf)
 {
-    using SP = StockhamPlan<T, LOGN, FusedE<T>::value>;
-    cpx<T> *o = static_cast<cpx<T> *>(buf);
-    int ns = SP::R0;
-    for (int p = 1; p < SP::P; p++) {
-        const int off = SP::twiddle_offset(p);
-        for (int r = 1; r < SP::E; r++)
-            for (int m = 0; m < ns; m++)
-                forward_root<T>((long long)m * r, (long long)ns * SP::E,
-                                &o[off + (r - 1) * ns + m].x, &o[off + (r - 1) * ns + m].y);
-        ns *= SP::E;
-    }
+    stockham_fill_twiddles<T, LOGN, FusedE<T>::value>(
+        static_cast<cpx<T> *>(buf), [](long long k, long long M, cpx<T> *w) { forward_root<T>(k, M, &w->x, &w->y); });
 }
 
 struct Entry {

@@ -99,25 +99,26 @@ __device__ __forceinline__ void st_c(cpx<T> *p, cpx<T> a)
 }
 
 // ---------------------------------------------------------------------------
-// Multiplication by the compile-time root W_16^k = exp(-2 pi i k / 16)
+// Multiplication by the compile-time root W_32^k = exp(-2 pi i k / 32)
 // (forward) or its conjugate (inverse).  Trivial roots cost no multiply,
 // the 45-degree roots two.  Constants are the correctly rounded values of
-// cos(pi/8), sin(pi/8) and sqrt(1/2).
-template <typename T>
-struct K16 {
-    static constexpr double C1 = 0.92387953251128675613;  // cos(pi/8)
-    static constexpr double S1 = 0.38268343236508977173;  // sin(pi/8)
-    static constexpr double R2 = 0.70710678118654752440;  // sqrt(1/2)
-};
+// cos(pi m / 16), m = 0..8.
 
-// cos(2 pi k / 16) for k in [0, 16)
-template <typename T>
-__host__ __device__ constexpr T cos16(int k)
+// cos(2 pi k / 32) for any integer k
+__host__ __device__ constexpr double cos32d(int k)
 {
-    return k == 0 ? (T)1 : k == 1 ? (T)K16<T>::C1 : k == 2 ? (T)K16<T>::R2 : k == 3 ? (T)K16<T>::S1
-         : k == 4 ? (T)0 : k == 5 ? -(T)K16<T>::S1 : k == 6 ? -(T)K16<T>::R2 : k == 7 ? -(T)K16<T>::C1
-         : k == 8 ? (T)-1 : k == 9 ? -(T)K16<T>::C1 : k == 10 ? -(T)K16<T>::R2 : k == 11 ? -(T)K16<T>::S1
-         : k == 12 ? (T)0 : k == 13 ? (T)K16<T>::S1 : k == 14 ? (T)K16<T>::R2 : (T)K16<T>::C1;
+    k = ((k % 32) + 32) % 32;
+    if (k > 16) k = 32 - k;
+    if (k > 8) return -cos32d(16 - k);
+    return k == 0 ? 1.0
+         : k == 1 ? 0.98078528040323044913
+         : k == 2 ? 0.92387953251128675613
+         : k == 3 ? 0.83146961230254523708
+         : k == 4 ? 0.70710678118654752440
+         : k == 5 ? 0.55557023301960222474
+         : k == 6 ? 0.38268343236508977173
+         : k == 7 ? 0.19509032201612826785
+                  : 0.0;
 }
 
 // compile-time loop: f(std::integral_constant<int, I>) for I in [B, E)
@@ -131,31 +132,31 @@ __device__ __forceinline__ void static_for(F &&f)
 }
 
 template <int K, bool INV, typename T>
-__device__ __forceinline__ cpx<T> rot16(cpx<T> a)
+__device__ __forceinline__ cpx<T> rot32(cpx<T> a)
 {
     // exponent of the effective forward root after folding direction
-    constexpr int k = INV ? ((16 - (K % 16)) % 16) : (K % 16);
-    constexpr T r2 = (T)K16<T>::R2;
+    constexpr int k = INV ? ((32 - (K % 32)) % 32) : (K % 32);
+    constexpr T r2 = (T)cos32d(4);
     if constexpr (k == 0) return a;
-    else if constexpr (k == 4) return {a.y, -a.x};     // * (-i)
-    else if constexpr (k == 8) return {-a.x, -a.y};    // * (-1)
-    else if constexpr (k == 12) return {-a.y, a.x};    // * (+i)
-    else if constexpr (k == 2) return {r2 * (a.x + a.y), r2 * (a.y - a.x)};      // (r2, -r2)
-    else if constexpr (k == 6) return {r2 * (a.y - a.x), -r2 * (a.x + a.y)};     // (-r2, -r2)
-    else if constexpr (k == 10) return {-r2 * (a.x + a.y), r2 * (a.x - a.y)};    // (-r2, r2)
-    else if constexpr (k == 14) return {r2 * (a.x - a.y), r2 * (a.x + a.y)};     // (r2, r2)
+    else if constexpr (k == 8) return {a.y, -a.x};     // * (-i)
+    else if constexpr (k == 16) return {-a.x, -a.y};   // * (-1)
+    else if constexpr (k == 24) return {-a.y, a.x};    // * (+i)
+    else if constexpr (k == 4) return {r2 * (a.x + a.y), r2 * (a.y - a.x)};      // (r2, -r2)
+    else if constexpr (k == 12) return {r2 * (a.y - a.x), -r2 * (a.x + a.y)};    // (-r2, -r2)
+    else if constexpr (k == 20) return {-r2 * (a.x + a.y), r2 * (a.x - a.y)};    // (-r2, r2)
+    else if constexpr (k == 28) return {r2 * (a.x - a.y), r2 * (a.x + a.y)};     // (r2, r2)
     else {
-        // general root: cos(2 pi k/16), -sin(2 pi k/16)
-        constexpr T wr = cos16<T>(k);
-        constexpr T wi = -cos16<T>((k + 12) % 16);  // sin(t) = cos(t - pi/2)
+        // general root: cos(2 pi k/32), -sin(2 pi k/32); sin(t) = cos(t - pi/2)
+        constexpr T wr = (T)cos32d(k);
+        constexpr T wi = (T)(-cos32d(k - 8));
         return {a.x * wr - a.y * wi, a.x * wi + a.y * wr};
     }
 }
 
 // ---------------------------------------------------------------------------
-// In-register DFT of R points (R = 1, 2, 4, 8, 16), natural order in and
-// out, stride-1 over the array v.  R = 8 and 16 are split as A x B
-// (A = 2 or 4): n = n1 + A*n2, k = k1 + B*k2,
+// In-register DFT of R points (R = 1, 2, 4, 8, 16, 32), natural order in
+// and out, stride-1 over the array v.  R >= 8 is split as A x B
+// (A = 2 for R = 8, else 4): n = n1 + A*n2, k = k1 + B*k2,
 //   X[k1 + B k2] = sum_n1 W_A^(n1 k2) W_R^(n1 k1) sum_n2 x[n1 + A n2] W_B^(n2 k1)
 template <int R, bool INV, typename T>
 __device__ __forceinline__ void dft(cpx<T> *v)
@@ -176,7 +177,7 @@ __device__ __forceinline__ void dft(cpx<T> *v)
         v[1] = d02 + jd13;
         v[3] = d02 - jd13;
     } else {
-        constexpr int A = (R == 16) ? 4 : 2;
+        constexpr int A = (R >= 16) ? 4 : 2;
         constexpr int B = R / A;
         cpx<T> y[A][B];
 #pragma unroll
@@ -185,14 +186,14 @@ __device__ __forceinline__ void dft(cpx<T> *v)
             for (int n2 = 0; n2 < B; n2++) y[n1][n2] = v[n1 + A * n2];
             dft<B, INV, T>(y[n1]);
         }
-        // inner twiddles W_R^(n1 k1) = W_16^(n1 k1 16/R)
-        constexpr int S = 16 / R;
+        // inner twiddles W_R^(n1 k1) = W_32^(n1 k1 32/R)
+        constexpr int S = 32 / R;
         static_for<0, B>([&](auto k1c) {
             constexpr int k1 = decltype(k1c)::value;
             cpx<T> z[A];
             static_for<0, A>([&](auto n1c) {
                 constexpr int n1 = decltype(n1c)::value;
-                z[n1] = rot16<n1 * k1 * S, INV, T>(y[n1][k1]);
+                z[n1] = rot32<n1 * k1 * S, INV, T>(y[n1][k1]);
             });
             dft<A, INV, T>(z);
 #pragma unroll

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <cstddef>
+#include <functional>
 #include <string>
 
 #include "../../include/genfft_gb300.h"
@@ -38,6 +39,6 @@ cudaError_t launch_fused_c2c(int dtype, int logn, int inverse, const FusedC2CArg
 // Returns a device pointer to the table made by `fill` (count complex
 // elements of dtype), cached per (device, key) for the process lifetime.
 const void *cached_table(const std::string &key, int dtype, size_t count,
-                         void (*fill)(int, int, void *), int logn);
+                         const std::function<void(void *)> &fill);
 
 }  // namespace gfft

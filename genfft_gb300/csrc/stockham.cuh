@@ -53,13 +53,14 @@ struct StockhamPlan {
 
 // Runs all passes of one transform held by thread t of its group.
 //   v   : E points per thread, v[q] = x[t + q G] on entry, X[t + q G] on exit
-//   sm  : this group's shared-memory region (SMEM elements)
+//   at  : at(i) is the shared-memory slot of element i of this transform
+//         (only touched when P > 1)
 //   tw  : the plan's twiddle table (StockhamPlan::TW elements)
-// SYNC() must synchronise every thread that shares the barrier (the whole
-// CTA, or the group).
-template <typename T, int LOGN, int E_, bool INV, typename Sync>
+// SYNC() must synchronise every thread that shares the shared memory (the
+// whole CTA, or the group).
+template <typename T, int LOGN, int E_, bool INV, typename At, typename Sync>
 __device__ __forceinline__ void stockham_run(cpx<T> (&v)[StockhamPlan<T, LOGN, E_>::E], int t,
-                                             cpx<T> *sm, const cpx<T> *__restrict__ tw, Sync SYNC)
+                                             At at, const cpx<T> *__restrict__ tw, Sync SYNC)
 {
     using SP = StockhamPlan<T, LOGN, E_>;
     constexpr int E = SP::E, G = SP::G, P = SP::P, R0 = SP::R0;
@@ -77,7 +78,7 @@ __device__ __forceinline__ void stockham_run(cpx<T> (&v)[StockhamPlan<T, LOGN, E
         } else {
             const int j = t + m * G;
 #pragma unroll
-            for (int r = 0; r < R0; r++) sm[spad<T>(j * R0 + r)] = u[r];
+            for (int r = 0; r < R0; r++) at(j * R0 + r) = u[r];
         }
     }
 
@@ -88,7 +89,7 @@ __device__ __forceinline__ void stockham_run(cpx<T> (&v)[StockhamPlan<T, LOGN, E
         constexpr int off = SP::twiddle_offset(p);
         SYNC();
 #pragma unroll
-        for (int q = 0; q < E; q++) v[q] = sm[spad<T>(t + q * G)];
+        for (int q = 0; q < E; q++) v[q] = at(t + q * G);
         const int jm = t % Ns;  // Ns <= G, so j = t
         const cpx<T> *twp = tw + off + jm;
 #pragma unroll
@@ -98,9 +99,27 @@ __device__ __forceinline__ void stockham_run(cpx<T> (&v)[StockhamPlan<T, LOGN, E
             SYNC();
             const int base = (t / Ns) * Ns * E + jm;
 #pragma unroll
-            for (int r = 0; r < E; r++) sm[spad<T>(base + r * Ns)] = v[r];
+            for (int r = 0; r < E; r++) at(base + r * Ns) = v[r];
         }
     });
 }
+
+// host-side fill of a StockhamPlan twiddle table (TW complex elements)
+template <typename T, int LOGN, int E_, typename Root>
+void stockham_fill_twiddles(cpx<T> *o, Root root)
+{
+    using SP = StockhamPlan<T, LOGN, E_>;
+    int ns = SP::R0;
+    for (int p = 1; p < SP::P; p++) {
+        const int off = SP::twiddle_offset(p);
+        for (int r = 1; r < SP::E; r++)
+            for (int m = 0; m < ns; m++)
+                root((long long)m * r, (long long)ns * SP::E, &o[off + (r - 1) * ns + m]);
+        ns *= SP::E;
+    }
+}
+
+// bit reversal of the low `bits` bits
+__device__ __forceinline__ int bitrev(int i, int bits) { return bits ? (int)(__brev((unsigned)i) >> (32 - bits)) : 0; }
 
 }  // namespace gfft

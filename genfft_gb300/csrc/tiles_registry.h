@@ -1,0 +1,44 @@
+// tiles_registry.h -- host-side registry of the tile-kernel instantiations
+// (column pass, row pass) so the planner can pick one by (dtype, variant,
+// log2 length, columns per tile).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+
+namespace gfft {
+
+enum TileVariant {
+    TILE_COL_TW4 = 0,     // column pass of the four-step split (with W_N twiddle)
+    TILE_COL_PLAIN = 1,   // column FFT, natural-order input
+    TILE_COL_BITREV = 2,  // column FFT, bit-reversed row order on input
+    TILE_ROW_XPOSE = 3    // row pass with transposed store
+};
+
+struct TileKernel {
+    const void *fwd = nullptr, *inv = nullptr;
+    int threads = 0;
+    size_t smem = 0;
+    size_t twcount = 0;
+    void (*fill)(void *) = nullptr;  // Stockham twiddles for the L-point sub-FFT
+    int elem_bytes = 8;              // sizeof one complex element
+};
+
+// register / look up (returns nullptr when not instantiated)
+void tile_register(int dtype, int variant, int logl, int c, const TileKernel &k);
+const TileKernel *tile_find(int dtype, int variant, int logl, int c);
+// widest registered column count <= max_c (0 if none)
+int tile_widest(int dtype, int variant, int logl, int max_c);
+
+// Launch over tiles x nbatch CTAs (the batch is split into launches of at
+// most 65535 items).  Strides and distances are in complex elements.
+cudaError_t launch_colpass(const TileKernel &k, int inverse, long long tiles, long long nbatch,
+                           const void *in, void *out, long long ncols, long long ld_in, long long ld_out,
+                           long long idist, long long odist, const void *tw, const void *tw_lo,
+                           const void *tw_hi, int lo_bits, unsigned nmask, cudaStream_t st);
+cudaError_t launch_rowpass(const TileKernel &k, int inverse, long long tiles, long long nbatch,
+                           const void *in, void *out, long long nrows, long long ld_in, long long ostride,
+                           long long idist, long long odist, const void *tw, cudaStream_t st);
+
+}  // namespace gfft
