@@ -14,7 +14,9 @@ from __future__ import annotations
 import ctypes
 import os
 
-__all__ = ["GFFTError", "Plan", "lib", "lib_path", "fft", "ifft", "F32", "F64"]
+__all__ = ["GFFTError", "Plan", "lib", "lib_path", "fft", "ifft", "fft_no_scramble", "rfft", "fft_real_input",
+           "fft_interleave", "separate_2x", "dit", "fft_vert", "fft_vert_no_scramble", "fft2", "rfft2",
+           "rfft2_2x", "F32", "F64"]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "libgenfft_gb300.so")
@@ -53,7 +55,19 @@ SIGNATURES = {
     "gfft_exec": [_P, _I, _P, _P, _P],
     "gfft_exec_host": [_P, _I, _P, _P],
     "gfft_plan_launches": [_P, ctypes.POINTER(_I)],
+    "gfft_plan_workspace_size": [_P, ctypes.POINTER(ctypes.c_size_t)],
     "gfft_fft_transform": [_I, _I, _LL, _I, _P, _P, _P],
+    "gfft_fft_transform_no_scramble": [_I, _I, _LL, _I, _P, _P],
+    "gfft_fft_transform_real": [_I, _I, _LL, _P, _P, _P],
+    "gfft_fft_transform_interleave": [_I, _I, _P, _P, _P, _P],
+    "gfft_vert_transform": [_I, _I, _I, _P, _LL, _P, _LL, _I, _P],
+    "gfft_vert_transform_no_scramble": [_I, _I, _I, _P, _LL, _I, _P],
+    "gfft_dit_apply": [_I, _I, _P, _P, _I, _P],
+    "gfft_fft2d_transform": [_I, _I, _I, _I, _P, _LL, _P, _LL, _P],
+    "gfft_real_fft_forward": [_I, _I, _LL, _P, _P, _I, _P],
+    "gfft_real_fft2d_forward": [_I, _I, _I, _P, _LL, _P, _LL, _P],
+    "gfft_real_fft2d_forward_2x": [_I, _I, _I, _P, _LL, _P, _LL, _P, _LL, _P],
+    "gfft_separate_2x_real_fft": [_I, _I, _P, _P, _P, _P],
     "gfft_status_string": [_I],
     "gfft_last_error": [],
     "gfft_version": [],
@@ -172,3 +186,143 @@ def fft(x, inverse: bool = False, out=None):
 def ifft(x, out=None):
     """Unscaled inverse: ifft(fft(x)) == n * x."""
     return fft(x, True, out)
+
+
+def _cdtype_for_real(x):
+    import torch
+    return torch.complex64 if x.dtype == torch.float32 else torch.complex128
+
+
+def fft_no_scramble(x, inverse: bool = False):
+    """In place on x: bit-reversed input order, natural output
+    (FFT<T>::transform_no_scramble, fft.h:69-73)."""
+    _check_cuda_tensor(x)
+    n = x.shape[-1]
+    _check(lib().gfft_fft_transform_no_scramble(_dtype_code(x), n, x.numel() // n, int(inverse), x.data_ptr(),
+                                                _stream_ptr()))
+    return x
+
+
+def rfft(x, half: bool = True, out=None):
+    """RealFFT<T>::forward over the last dimension (FFTReal.h:204-213):
+    n reals -> n/2+1 bins (half) or the full Hermitian n bins."""
+    import torch
+    _check_cuda_tensor(x)
+    if x.dtype not in (torch.float32, torch.float64):
+        raise TypeError("rfft expects float32/float64")
+    n = x.shape[-1]
+    batch = x.numel() // n
+    m = n // 2 + 1 if half else n
+    if out is None:
+        out = torch.empty(*x.shape[:-1], m, dtype=_cdtype_for_real(x), device=x.device)
+    p = Plan(KIND_R2C, _dtype_code(x), n, 0, batch, FLAG_HALF_SPECTRUM if half else 0, 0, n, 0, m)
+    p.exec(out, x)
+    return out
+
+
+def fft_real_input(x):
+    """FFT<T>::transform_real (fft.h:90-94): full complex spectrum of reals."""
+    import torch
+    _check_cuda_tensor(x)
+    n = x.shape[-1]
+    out = torch.empty(*x.shape, dtype=_cdtype_for_real(x), device=x.device)
+    _check(lib().gfft_fft_transform_real(_dtype_code(x), n, x.numel() // n, out.data_ptr(), x.data_ptr(),
+                                         _stream_ptr()))
+    return out
+
+
+def fft_interleave(a, b):
+    """FFT<T>::transform_interleave (fft.h:100-105): FFT of a + i b (1D)."""
+    import torch
+    _check_cuda_tensor(a, "a")
+    _check_cuda_tensor(b, "b")
+    n = a.shape[-1]
+    out = torch.empty(n, dtype=_cdtype_for_real(a), device=a.device)
+    _check(lib().gfft_fft_transform_interleave(_dtype_code(a), n, out.data_ptr(), a.data_ptr(), b.data_ptr(),
+                                               _stream_ptr()))
+    return out
+
+
+def separate_2x(z):
+    """separate_2x_real_FFT (FFTReal.h:34-66) -> (X, Y)."""
+    import torch
+    _check_cuda_tensor(z, "z")
+    n = z.shape[-1]
+    a, b = torch.empty_like(z), torch.empty_like(z)
+    _check(lib().gfft_separate_2x_real_fft(_dtype_code(z), n, a.data_ptr(), b.data_ptr(), z.data_ptr(),
+                                           _stream_ptr()))
+    return a, b
+
+
+def dit(z, n: int, half: bool):
+    """DIT<T>(n).apply on an n/2-point spectrum z (fft.h:180-188); returns
+    an n-element buffer (only n/2+1 written when half)."""
+    import torch
+    _check_cuda_tensor(z, "z")
+    out = torch.zeros(n, dtype=z.dtype, device=z.device)
+    buf = torch.zeros(n, dtype=z.dtype, device=z.device)
+    buf[: z.shape[-1]] = z
+    _check(lib().gfft_dit_apply(_dtype_code(z), n, out.data_ptr(), buf.data_ptr(), int(half), _stream_ptr()))
+    return out
+
+
+def fft_vert(x, inverse: bool = False, out=None):
+    """FFTVert<T>(rows).transform on an [rows, cols] tensor (fft.h:145-150)."""
+    import torch
+    _check_cuda_tensor(x)
+    rows, cols = x.shape
+    if out is None:
+        out = torch.empty_like(x)
+    _check(lib().gfft_vert_transform(_dtype_code(x), rows, int(inverse), out.data_ptr(), cols, x.data_ptr(),
+                                     cols, cols, _stream_ptr()))
+    return out
+
+
+def fft_vert_no_scramble(x, inverse: bool = False):
+    """FFTVert<T>::transform_no_scramble in place (rows bit-reversed)."""
+    _check_cuda_tensor(x)
+    rows, cols = x.shape
+    _check(lib().gfft_vert_transform_no_scramble(_dtype_code(x), rows, int(inverse), x.data_ptr(), cols, cols,
+                                                 _stream_ptr()))
+    return x
+
+
+def fft2(x, inverse: bool = False, out=None):
+    """FFT2D<T>(W, H).transform on [..., H, W] (fft.h:213-218); batched over
+    leading dimensions through a plan."""
+    import torch
+    _check_cuda_tensor(x)
+    H, W = x.shape[-2:]
+    batch = x.numel() // (H * W)
+    if out is None:
+        out = torch.empty_like(x)
+    p = Plan(KIND_C2C_2D, _dtype_code(x), W, H, batch)
+    p.exec(out, x, inverse)
+    return out
+
+
+def rfft2(x, half: bool = False, out=None):
+    """RealFFT2D<T>(W, H).forward on [..., H, W] reals (FFTReal.h:83-104):
+    full-width Hermitian [H, W] output, or [H, W/2+1] when half."""
+    import torch
+    _check_cuda_tensor(x)
+    H, W = x.shape[-2:]
+    batch = x.numel() // (H * W)
+    m = W // 2 + 1 if half else W
+    if out is None:
+        out = torch.empty(*x.shape[:-1], m, dtype=_cdtype_for_real(x), device=x.device)
+    p = Plan(KIND_R2C_2D, _dtype_code(x), W, H, batch, FLAG_HALF_SPECTRUM if half else 0, W, H * W, m, H * m)
+    p.exec(out, x)
+    return out
+
+
+def rfft2_2x(a, b):
+    """RealFFT2D<T>::forward_2x (FFTReal.h:114-118): 2D FFT of a + i b."""
+    import torch
+    _check_cuda_tensor(a, "a")
+    _check_cuda_tensor(b, "b")
+    H, W = a.shape
+    out = torch.empty(H, W, dtype=_cdtype_for_real(a), device=a.device)
+    _check(lib().gfft_real_fft2d_forward_2x(_dtype_code(a), W, H, out.data_ptr(), W, a.data_ptr(), W,
+                                            b.data_ptr(), W, _stream_ptr()))
+    return out

@@ -1,6 +1,6 @@
-// api.cpp -- the C ABI of libgenfft_gb300.so: validation, plans, the plan
-// cache behind the reference-shaped entry points, twiddle-table cache and
-// the host-buffer execution path.
+// api.cpp -- the C ABI of libgenfft_gb300.so: validation, plan creation per
+// gfft_kind, execution, the plan cache behind the reference-shaped entry
+// points, the twiddle-table cache and the host-buffer path.
 //
 // The reference has no C ABI; its backend seam is the factory functions
 // backend::GetImpl / GetVertImpl / GetDITImpl (FFTBackend.h:15-45) that
@@ -9,11 +9,9 @@
 // (the reference's GetInstance is not thread-safe, FFTLevel.h:76-88).
 #include <cuda_runtime.h>
 
-#include <cstdarg>
-#include <cstdio>
-#include <cstdlib>
-#include <cstring>
 #include <algorithm>
+#include <cstdint>
+#include <cstring>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -22,52 +20,13 @@
 #include <vector>
 
 #include "internal.h"
-#include "tiles_registry.h"
-#include "twiddle.h"
-
-enum { ALGO_NONE = 0, ALGO_FUSED = 1, ALGO_FOURSTEP = 2 };
-
-struct gfft_plan_s {
-    gfft_desc d;
-    int device = 0;
-    int logn0 = 0, logn1 = 0;
-    int algo = ALGO_NONE;
-    const void *tw = nullptr; // fused: device twiddle table (cached, not owned)
-    int launches = 0;
-    // four-step (N = A * B): column pass over B columns of A points, row
-    // pass over A rows of B points; `group` transforms per launch pair so
-    // the intermediate (group * N elements) stays in L2
-    int logA = 0, logB = 0;
-    const gfft::TileKernel *kcol = nullptr, *krow = nullptr;
-    int ccol = 0, crow = 0;
-    const void *tw_col = nullptr, *tw_row = nullptr, *tw_lo = nullptr, *tw_hi = nullptr;
-    int lo_bits = 0;
-    long long group = 0;
-    void *ws = nullptr;
-    size_t ws_bytes = 0;
-    unsigned magic = 0x6766u;
-    // host-path staging (owned, lazily allocated)
-    std::mutex host_mu;
-    void *stage[3] = {nullptr, nullptr, nullptr};
-    void *stage_out[3] = {nullptr, nullptr, nullptr};
-    size_t stage_bytes_in = 0, stage_bytes_out = 0;
-    cudaStream_t host_streams[3] = {nullptr, nullptr, nullptr};
-};
+#include "plan.h"
 
 namespace gfft {
 
 namespace {
 thread_local std::string g_last_error;
-
-bool is_pow2(long long n) { return n > 0 && (n & (n - 1)) == 0; }
-int ilog2ll(long long n)
-{
-    int l = 0;
-    while ((1LL << l) < n) l++;
-    return l;
 }
-size_t cplx_bytes(int dtype) { return dtype == GFFT_F64 ? 16 : 8; }
-}  // namespace
 
 void fail(gfft_status st, const std::string &msg) { throw Error{st, msg}; }
 
@@ -96,8 +55,7 @@ static void check_device()
     if (!it->second) fail(GFFT_ERR_ARCH, "libgenfft_gb300 is built for sm_103a (GB300) only");
 }
 
-const void *cached_table(const std::string &key, int dtype, size_t count,
-                         const std::function<void(void *)> &fill)
+const void *cached_table(const std::string &key, int dtype, size_t count, const std::function<void(void *)> &fill)
 {
     static std::mutex mu;
     static std::map<std::pair<int, std::string>, void *> cache;
@@ -124,173 +82,237 @@ const void *cached_table(const std::string &key, int dtype, size_t count,
 // ---------------------------------------------------------------------------
 // planning
 
+static size_t real_bytes(int dtype) { return dtype == GFFT_F64 ? 8 : 4; }
+
 static void validate_desc(const gfft_desc &d)
 {
+    if (d.kind < GFFT_KIND_C2C || d.kind > GFFT_KIND_VERT) fail(GFFT_ERR_INVALID_VALUE, "unknown transform kind");
     if (d.dtype != GFFT_F32 && d.dtype != GFFT_F64) fail(GFFT_ERR_INVALID_VALUE, "dtype must be GFFT_F32 or GFFT_F64");
     if (d.mode != GFFT_MODE_PLAIN) fail(GFFT_ERR_INVALID_VALUE, "unknown mode");
     if (d.batch < 1) fail(GFFT_ERR_INVALID_SIZE, "batch must be >= 1");
     if (!is_pow2(d.n0)) fail(GFFT_ERR_INVALID_SIZE, "size must be a power of two >= 1 (README.txt:10-11)");
+    if (d.kind == GFFT_KIND_C2C_2D || d.kind == GFFT_KIND_R2C_2D) {
+        if (!is_pow2(d.n1)) fail(GFFT_ERR_INVALID_SIZE, "2D height must be a power of two >= 1");
+    } else if (d.kind == GFFT_KIND_VERT) {
+        if (d.n1 < 1) fail(GFFT_ERR_INVALID_SIZE, "column count must be >= 1");
+    }
+    if (d.n0 > (1LL << 26) || d.n1 > (1LL << 26)) fail(GFFT_ERR_INVALID_SIZE, "size above 2^26");
     if (d.istride < 0 || d.ostride < 0 || d.idist < 0 || d.odist < 0)
         fail(GFFT_ERR_INVALID_VALUE, "strides and distances must be >= 0");
-    if (d.flags & ~(unsigned)(GFFT_FLAG_HALF_SPECTRUM | GFFT_FLAG_BITREV_INPUT))
-        fail(GFFT_ERR_INVALID_VALUE, "unknown flag bits");
+    const unsigned known = GFFT_FLAG_HALF_SPECTRUM | GFFT_FLAG_BITREV_INPUT;
+    if (d.flags & ~known) fail(GFFT_ERR_INVALID_VALUE, "unknown flag bits");
+    if ((d.flags & GFFT_FLAG_HALF_SPECTRUM) && d.kind != GFFT_KIND_R2C && d.kind != GFFT_KIND_R2C_2D)
+        fail(GFFT_ERR_INVALID_VALUE, "GFFT_FLAG_HALF_SPECTRUM applies to real-input kinds only");
+    if ((d.flags & GFFT_FLAG_BITREV_INPUT) && d.kind != GFFT_KIND_C2C && d.kind != GFFT_KIND_VERT)
+        fail(GFFT_ERR_INVALID_VALUE, "GFFT_FLAG_BITREV_INPUT applies to C2C and VERT only");
 }
 
-static const void *tile_table(int dtype, const TileKernel *k, int logl, int c)
+// fill in default strides/distances (all in elements of the array's type)
+static void apply_defaults(gfft_desc &d)
 {
-    return cached_table("tile/" + std::to_string(dtype) + "/" + std::to_string(logl) + "/" + std::to_string(c) +
-                            "/" + std::to_string(k->threads),
-                        dtype, k->twcount, [k](void *buf) { k->fill(buf); });
-}
-
-// W_N^e split as tw_hi[e >> lo_bits] * tw_lo[e & (2^lo_bits - 1)]
-static void four_step_tables(gfft_plan_s &p, int logn)
-{
-    const int dtype = p.d.dtype;
-    const int lo_bits = (logn + 1) / 2;
-    const long long N = 1LL << logn;
-    p.lo_bits = lo_bits;
-    auto fill = [dtype, N](long long count, long long mul) {
-        return [dtype, N, count, mul](void *buf) {
-            for (long long e = 0; e < count; e++) {
-                if (dtype == GFFT_F32) {
-                    float *o = static_cast<float *>(buf);
-                    forward_root<float>(e * mul, N, &o[2 * e], &o[2 * e + 1]);
-                } else {
-                    double *o = static_cast<double *>(buf);
-                    forward_root<double>(e * mul, N, &o[2 * e], &o[2 * e + 1]);
-                }
-            }
-        };
-    };
-    const std::string key = "4s/" + std::to_string(dtype) + "/" + std::to_string(logn);
-    p.tw_lo = cached_table(key + "/lo", dtype, 1LL << lo_bits, fill(1LL << lo_bits, 1));
-    p.tw_hi = cached_table(key + "/hi", dtype, N >> lo_bits, fill(N >> lo_bits, 1LL << lo_bits));
-}
-
-static long long env_ll(const char *name, long long dflt)
-{
-    const char *v = std::getenv(name);
-    return (v && *v) ? std::atoll(v) : dflt;
-}
-
-static void plan_fourstep(gfft_plan_s &p, int logn)
-{
-    const gfft_desc &d = p.d;
-    if (d.istride != 1 || d.ostride != 1)
-        fail(GFFT_ERR_UNSUPPORTED, "sizes above the fused limit need unit element strides");
-    if (logn > 24) fail(GFFT_ERR_INVALID_SIZE, "size above 2^24 is not supported");
-    // A (column-FFT length) and B (row-FFT length), both at most 2^12
-    p.logA = logn / 2;
-    p.logB = logn - p.logA;
-    const long long maxc = env_ll("GFFT_TILE_MAXC", 16);
-    p.ccol = tile_widest(d.dtype, TILE_COL_TW4, p.logA, (int)maxc);
-    p.crow = tile_widest(d.dtype, TILE_ROW_XPOSE, p.logB, (int)maxc);
-    if (!p.ccol || !p.crow) fail(GFFT_ERR_UNSUPPORTED, "no tile kernel for this size");
-    p.kcol = tile_find(d.dtype, TILE_COL_TW4, p.logA, p.ccol);
-    p.krow = tile_find(d.dtype, TILE_ROW_XPOSE, p.logB, p.crow);
-    p.tw_col = tile_table(d.dtype, p.kcol, p.logA, p.ccol);
-    p.tw_row = tile_table(d.dtype, p.krow, p.logB, p.crow);
-    four_step_tables(p, logn);
-    // group so the intermediate fits comfortably in the 129 MB L2
-    const long long N = 1LL << logn;
-    const long long l2_budget = env_ll("GFFT_L2_BUDGET_MB", 48) << 20;
-    p.group = std::max<long long>(1, l2_budget / (N * (long long)cplx_bytes(d.dtype)));
-    p.group = std::min(p.group, std::max<long long>(1, d.batch));
-    p.ws_bytes = (size_t)(p.group * N) * cplx_bytes(d.dtype);
-    check_cuda(cudaMalloc(&p.ws, p.ws_bytes), "cudaMalloc(workspace)");
-    p.algo = ALGO_FOURSTEP;
-    p.launches = 2 * (int)((d.batch + p.group - 1) / p.group);
-}
-
-static void plan_c2c(gfft_plan_s &p)
-{
-    const gfft_desc &d = p.d;
-    if (d.flags & GFFT_FLAG_BITREV_INPUT) fail(GFFT_ERR_UNSUPPORTED, "bit-reversed input not built yet");
-    p.logn0 = ilog2ll(d.n0);
-    if (p.logn0 <= fused_max_logn(d.dtype)) {
-        const int logn = p.logn0, dtype = d.dtype;
-        p.algo = ALGO_FUSED;
-        p.launches = 1;
-        p.tw = cached_table("fused/" + std::to_string(dtype) + "/" + std::to_string(logn), dtype,
-                            fused_twiddle_count(dtype, logn),
-                            [dtype, logn](void *buf) { fused_twiddle_fill(dtype, logn, buf); });
-        return;
+    const bool half = (d.flags & GFFT_FLAG_HALF_SPECTRUM) != 0;
+    switch (d.kind) {
+    case GFFT_KIND_C2C:
+        if (!d.istride) d.istride = 1;
+        if (!d.ostride) d.ostride = 1;
+        if (!d.idist) d.idist = d.n0 * d.istride;
+        if (!d.odist) d.odist = d.n0 * d.ostride;
+        break;
+    case GFFT_KIND_R2C:
+        d.istride = d.ostride = 1;
+        if (!d.idist) d.idist = d.n0;
+        if (!d.odist) d.odist = half ? d.n0 / 2 + 1 : d.n0;
+        break;
+    case GFFT_KIND_C2C_2D:  // istride/ostride are row strides
+        if (!d.istride) d.istride = d.n0;
+        if (!d.ostride) d.ostride = d.n0;
+        if (!d.idist) d.idist = d.n1 * d.istride;
+        if (!d.odist) d.odist = d.n1 * d.ostride;
+        break;
+    case GFFT_KIND_R2C_2D:
+        if (!d.istride) d.istride = d.n0;
+        if (!d.ostride) d.ostride = half ? d.n0 / 2 + 1 : d.n0;
+        if (!d.idist) d.idist = d.n1 * d.istride;
+        if (!d.odist) d.odist = d.n1 * d.ostride;
+        break;
+    case GFFT_KIND_VERT:  // n0 rows, n1 columns, row strides
+        if (!d.istride) d.istride = d.n1;
+        if (!d.ostride) d.ostride = d.n1;
+        if (!d.idist) d.idist = d.n0 * d.istride;
+        if (!d.odist) d.odist = d.n0 * d.ostride;
+        break;
     }
-    plan_fourstep(p, p.logn0);
+}
+
+static void check_layout(const gfft_desc &d)
+{
+    const bool half = (d.flags & GFFT_FLAG_HALF_SPECTRUM) != 0;
+    switch (d.kind) {
+    case GFFT_KIND_R2C:
+        if (d.n0 > 1 && (d.idist % 2)) fail(GFFT_ERR_INVALID_VALUE, "R2C input distance must be even");
+        if (d.odist < (half ? d.n0 / 2 + 1 : d.n0)) fail(GFFT_ERR_INVALID_VALUE, "R2C output distance too small");
+        break;
+    case GFFT_KIND_C2C_2D:
+        if (d.istride < d.n0 || d.ostride < d.n0) fail(GFFT_ERR_INVALID_VALUE, "2D row stride below the width");
+        break;
+    case GFFT_KIND_R2C_2D:
+        if (d.n0 > 1 && (d.istride % 2)) fail(GFFT_ERR_INVALID_VALUE, "real 2D input row stride must be even");
+        if (d.istride < d.n0) fail(GFFT_ERR_INVALID_VALUE, "2D row stride below the width");
+        if (d.ostride < (half ? d.n0 / 2 + 1 : d.n0)) fail(GFFT_ERR_INVALID_VALUE, "2D output row stride too small");
+        break;
+    case GFFT_KIND_VERT:
+        if (d.istride < d.n1 || d.ostride < d.n1) fail(GFFT_ERR_INVALID_VALUE, "row stride below the column count");
+        break;
+    default:
+        break;
+    }
 }
 
 static gfft_plan_s *make_plan(const gfft_desc &in)
 {
     gfft_desc d = in;
     validate_desc(d);
-    if (d.istride == 0) d.istride = 1;
-    if (d.ostride == 0) d.ostride = 1;
+    apply_defaults(d);
+    check_layout(d);
     check_device();
     std::unique_ptr<gfft_plan_s> p(new gfft_plan_s());
     check_cuda(cudaGetDevice(&p->device), "cudaGetDevice");
-    switch (d.kind) {
-    case GFFT_KIND_C2C:
-        if (d.idist == 0) d.idist = d.n0 * d.istride;
-        if (d.odist == 0) d.odist = d.n0 * d.ostride;
-        p->d = d;
-        plan_c2c(*p);
-        break;
-    default:
-        fail(GFFT_ERR_UNSUPPORTED, "transform kind not built yet");
+    p->d = d;
+    const bool half = (d.flags & GFFT_FLAG_HALF_SPECTRUM) != 0;
+    const bool bitrev = (d.flags & GFFT_FLAG_BITREV_INPUT) != 0;
+    try {
+        switch (d.kind) {
+        case GFFT_KIND_C2C:
+            p->c2c.init(d.dtype, ilog2ll(d.n0), d.batch);
+            p->launches = p->c2c.launches(d.batch) + (bitrev ? 1 : 0);
+            break;
+        case GFFT_KIND_R2C:
+            p->r2c.init(d.dtype, ilog2ll(d.n0), half ? 1 : 0, d.batch);
+            p->launches = p->r2c.launches(d.batch);
+            break;
+        case GFFT_KIND_C2C_2D:
+            p->c2c.init(d.dtype, ilog2ll(d.n0), d.batch * d.n1);
+            p->col.init(d.dtype, ilog2ll(d.n1), TILE_COL_PLAIN);
+            p->launches = p->c2c.launches(d.batch * d.n1) + 1;
+            break;
+        case GFFT_KIND_R2C_2D:
+            p->r2c.init(d.dtype, ilog2ll(d.n0), 1, d.batch * d.n1);
+            p->col.init(d.dtype, ilog2ll(d.n1), half ? TILE_COL_PLAIN : TILE_COL_HERM);
+            p->launches = p->r2c.launches(d.batch * d.n1) + 1;
+            break;
+        case GFFT_KIND_VERT:
+            p->col.init(d.dtype, ilog2ll(d.n0), bitrev ? TILE_COL_BITREV : TILE_COL_PLAIN);
+            p->launches = 1;
+            break;
+        }
+    } catch (...) {
+        p->c2c.release();
+        p->r2c.release();
+        throw;
     }
     return p.release();
 }
 
-static void check_ptr(const void *ptr, int dtype, const char *name)
+static void check_ptr(const void *ptr, size_t align, const char *name)
 {
     if (!ptr) fail(GFFT_ERR_INVALID_VALUE, std::string(name) + " is NULL");
-    const uintptr_t a = dtype == GFFT_F64 ? 16 : 8;
-    if ((uintptr_t)ptr % a) fail(GFFT_ERR_ALIGN, std::string(name) + " is not aligned to its complex element");
+    if ((uintptr_t)ptr % align) fail(GFFT_ERR_ALIGN, std::string(name) + " is not aligned to its element type");
 }
 
-static void exec_plan(gfft_plan_s &p, int inverse, void *out, const void *in, cudaStream_t st,
-                      long long batch_override = -1)
+// per-call layout (reference-shaped entry points override the plan's)
+struct Layout {
+    long long batch, istride, idist, ostride, odist;
+};
+
+static Layout plan_layout(const gfft_plan_s &p)
+{
+    return Layout{p.d.batch, p.d.istride, p.d.idist, p.d.ostride, p.d.odist};
+}
+
+static bool overlaps(const void *a, size_t an, const void *b, size_t bn)
+{
+    const char *x = static_cast<const char *>(a), *y = static_cast<const char *>(b);
+    return x < y + bn && y < x + an;
+}
+
+static void exec_plan(gfft_plan_s &p, int inverse, void *out, const void *in, const Layout &L, cudaStream_t st)
 {
     const gfft_desc &d = p.d;
-    check_ptr(in, d.dtype, "in");
-    check_ptr(out, d.dtype, "out");
-    const long long batch = batch_override >= 0 ? batch_override : d.batch;
-    switch (p.algo) {
-    case ALGO_FUSED: {
-        FusedC2CArgs a{in, out, batch, d.idist, d.odist, d.istride, d.ostride, p.tw};
-        check_cuda(launch_fused_c2c(d.dtype, p.logn0, inverse, a, st), "launch fused C2C");
+    const size_t cb = cplx_bytes(d.dtype), rb = real_bytes(d.dtype);
+    const bool real_in = d.kind == GFFT_KIND_R2C || d.kind == GFFT_KIND_R2C_2D;
+    check_ptr(in, real_in ? rb : cb, "in");
+    check_ptr(out, cb, "out");
+    switch (d.kind) {
+    case GFFT_KIND_C2C:
+        if (d.flags & GFFT_FLAG_BITREV_INPUT) {
+            // transform_no_scramble (fft.h:69-73): permute to natural order in
+            // the output buffer, then transform in place
+            if (L.istride != 1 || L.ostride != 1 || L.idist != L.odist)
+                fail(GFFT_ERR_UNSUPPORTED, "bit-reversed input needs dense batches");
+            if (out != in)
+                check_cuda(cudaMemcpyAsync(out, in, (size_t)(L.batch * L.idist) * cb, cudaMemcpyDeviceToDevice, st),
+                           "copy");
+            check_cuda(launch_bitrev_swap(d.dtype, out, p.c2c.logn, L.batch, L.odist, st), "bit reversal");
+            p.c2c.run(inverse, out, out, L.batch, L.odist, L.odist, 1, 1, st);
+        } else {
+            p.c2c.run(inverse, in, out, L.batch, L.idist, L.odist, L.istride, L.ostride, st);
+        }
+        break;
+    case GFFT_KIND_R2C: {
+        if (inverse) fail(GFFT_ERR_UNSUPPORTED, "the real-input transform has no inverse (FFTReal.h:186-221)");
+        if (overlaps(in, (size_t)(L.batch * L.idist) * rb, out, (size_t)(L.batch * L.odist) * cb))
+            fail(GFFT_ERR_ALIAS, "real-input transform: output must not overlap the input");
+        p.r2c.run(in, out, L.batch, L.idist, L.odist, st);
         break;
     }
-    case ALGO_FOURSTEP: {
-        const long long A = 1LL << p.logA, B = 1LL << p.logB, N = A * B;
-        const size_t eb = cplx_bytes(d.dtype);
-        const unsigned nmask = (unsigned)(N - 1);
-        for (long long g0 = 0; g0 < batch; g0 += p.group) {
-            const long long nb = std::min(p.group, batch - g0);
-            const char *src = static_cast<const char *>(in) + (size_t)(g0 * d.idist) * eb;
-            char *dst = static_cast<char *>(out) + (size_t)(g0 * d.odist) * eb;
-            // column pass: B columns of A points, stride B, into the workspace
-            check_cuda(launch_colpass(*p.kcol, inverse, B / p.ccol, nb, src, p.ws, B, B, B, d.idist, N,
-                                      p.tw_col, p.tw_lo, p.tw_hi, p.lo_bits, nmask, st),
-                       "launch column pass");
-            // row pass: A rows of B points, stored transposed (stride A)
-            check_cuda(launch_rowpass(*p.krow, inverse, A / p.crow, nb, p.ws, dst, A, B, A, N, d.odist,
-                                      p.tw_row, st),
-                       "launch row pass");
+    case GFFT_KIND_C2C_2D: {
+        const long long W = d.n0, H = d.n1;
+        // row FFTs (FFT2D::scramble_row_fft, fft.h:229-241, in natural order)
+        if (L.idist == H * L.istride && L.odist == H * L.ostride) {
+            p.c2c.run(inverse, in, out, L.batch * H, L.istride, L.ostride, 1, 1, st);
+        } else {
+            for (long long b = 0; b < L.batch; b++)
+                p.c2c.run(inverse, static_cast<const char *>(in) + (size_t)(b * L.idist) * cb,
+                          static_cast<char *>(out) + (size_t)(b * L.odist) * cb, H, L.istride, L.ostride, 1, 1, st);
         }
+        // column FFTs in place (FFTVert::transform_no_scramble, fft.h:217)
+        p.col.run(inverse, out, out, W, L.ostride, L.ostride, L.batch, L.odist, L.odist, st);
+        break;
+    }
+    case GFFT_KIND_R2C_2D: {
+        if (inverse) fail(GFFT_ERR_UNSUPPORTED, "RealFFT2D has no inverse (FFTReal.h:127-130)");
+        const long long W = d.n0, H = d.n1;
+        if (overlaps(in, (size_t)(L.batch * L.idist) * rb, out, (size_t)(L.batch * L.odist) * cb))
+            fail(GFFT_ERR_ALIAS, "real 2D transform: output must not overlap the input (FFTReal.h:331)");
+        if (L.idist == H * L.istride && L.odist == H * L.ostride) {
+            p.r2c.run(in, out, L.batch * H, L.istride, L.ostride, st);
+        } else {
+            for (long long b = 0; b < L.batch; b++)
+                p.r2c.run(static_cast<const char *>(in) + (size_t)(b * L.idist) * rb,
+                          static_cast<char *>(out) + (size_t)(b * L.odist) * cb, H, L.istride, L.ostride, st);
+        }
+        // columns 0 .. W/2 (the non-redundant half), plus the Hermitian
+        // mirror of columns 1 .. W/2-1 for the full-width layout
+        p.col.run(0, out, out, W / 2 + 1, L.ostride, L.ostride, L.batch, L.odist, L.odist, st);
+        break;
+    }
+    case GFFT_KIND_VERT: {
+        const long long cols = d.n1;
+        if (out != in && overlaps(in, (size_t)(L.batch * L.idist) * cb, out, (size_t)(L.batch * L.odist) * cb))
+            fail(GFFT_ERR_ALIAS, "column transform: output must be the input or not overlap it");
+        p.col.run(inverse, in, out, cols, L.istride, L.ostride, L.batch, L.idist, L.odist, st);
         break;
     }
     default:
-        fail(GFFT_ERR_INVALID_PLAN, "plan has no algorithm");
+        fail(GFFT_ERR_INVALID_PLAN, "plan has no transform kind");
     }
 }
 
-// bytes of one transform's input / output, for host staging (dense plans)
-static void io_bytes(const gfft_plan_s &p, size_t *ib, size_t *ob)
+static void io_item_bytes(const gfft_plan_s &p, size_t *ib, size_t *ob)
 {
     const gfft_desc &d = p.d;
-    *ib = (size_t)d.idist * cplx_bytes(d.dtype);
+    const bool real_in = d.kind == GFFT_KIND_R2C || d.kind == GFFT_KIND_R2C_2D;
+    *ib = (size_t)d.idist * (real_in ? real_bytes(d.dtype) : cplx_bytes(d.dtype));
     *ob = (size_t)d.odist * cplx_bytes(d.dtype);
 }
 
@@ -298,13 +320,11 @@ static void exec_host(gfft_plan_s &p, int inverse, void *out, const void *in)
 {
     const gfft_desc &d = p.d;
     if (!in || !out) fail(GFFT_ERR_INVALID_VALUE, "NULL host buffer");
-    if (d.istride != 1 || d.ostride != 1 || d.idist != d.n0 || d.odist != d.n0)
-        fail(GFFT_ERR_UNSUPPORTED, "host execution needs dense batches");
     std::lock_guard<std::mutex> lk(p.host_mu);
     size_t ib, ob;
-    io_bytes(p, &ib, &ob);
+    io_item_bytes(p, &ib, &ob);
     // chunks of about 64 MB, at least one transform
-    long long per = std::max<long long>(1, (long long)((64u << 20) / std::max<size_t>(ib, 1)));
+    long long per = std::max<long long>(1, (long long)((64u << 20) / std::max<size_t>(std::max(ib, ob), 1)));
     per = std::min(per, d.batch);
     if (!p.stage[0] || p.stage_bytes_in < per * ib || p.stage_bytes_out < per * ob) {
         for (int i = 0; i < 3; i++) {
@@ -312,6 +332,7 @@ static void exec_host(gfft_plan_s &p, int inverse, void *out, const void *in)
             if (p.stage_out[i]) cudaFree(p.stage_out[i]);
             p.stage[i] = p.stage_out[i] = nullptr;
         }
+        p.stage_bytes_in = p.stage_bytes_out = 0;
         for (int i = 0; i < 3; i++) {
             check_cuda(cudaMalloc(&p.stage[i], per * ib), "cudaMalloc(stage)");
             check_cuda(cudaMalloc(&p.stage_out[i], per * ob), "cudaMalloc(stage)");
@@ -329,14 +350,31 @@ static void exec_host(gfft_plan_s &p, int inverse, void *out, const void *in)
         const int s = c % 3;
         cudaStream_t st = p.host_streams[s];
         check_cuda(cudaMemcpyAsync(p.stage[s], hin + b0 * ib, nb * ib, cudaMemcpyHostToDevice, st), "H2D");
-        exec_plan(p, inverse, p.stage_out[s], p.stage[s], st, nb);
+        Layout L = plan_layout(p);
+        L.batch = nb;
+        exec_plan(p, inverse, p.stage_out[s], p.stage[s], L, st);
         check_cuda(cudaMemcpyAsync(hout + b0 * ob, p.stage_out[s], nb * ob, cudaMemcpyDeviceToHost, st), "D2H");
     }
     for (int i = 0; i < 3; i++) check_cuda(cudaStreamSynchronize(p.host_streams[i]), "sync");
 }
 
-// cache of plans for the reference-shaped entry points: one per
-// (device, kind, dtype, n0, n1, flags); batch and pointers are per call
+static void destroy_plan(gfft_plan_s *p)
+{
+    for (int i = 0; i < 3; i++) {
+        if (p->stage[i]) cudaFree(p->stage[i]);
+        if (p->stage_out[i]) cudaFree(p->stage_out[i]);
+        if (p->host_streams[i]) cudaStreamDestroy(p->host_streams[i]);
+    }
+    p->c2c.release();
+    p->r2c.release();
+    p->magic = 0;
+    delete p;
+}
+
+// Cached plans for the reference-shaped entry points: one per (device,
+// kind, dtype, n0, n1, flags); batch, strides and pointers come per call.
+// Their workspace (four-step sizes only) is shared: calls that need one
+// must not overlap on different streams.
 static gfft_plan_s *cached_plan(int kind, int dtype, long long n0, long long n1, unsigned flags)
 {
     static std::mutex mu;
@@ -365,25 +403,35 @@ static gfft_plan_s *cached_plan(int kind, int dtype, long long n0, long long n1,
 
 using namespace gfft;
 
-#define GFFT_GUARD(body)                                               \
-    try {                                                              \
-        body;                                                          \
-        return GFFT_OK;                                                \
-    } catch (const Error &e) {                                         \
-        g_last_error = e.msg;                                          \
-        return e.status;                                               \
-    } catch (const std::bad_alloc &) {                                 \
-        g_last_error = "host allocation failed";                       \
-        return GFFT_ERR_ALLOC;                                         \
-    } catch (...) {                                                    \
-        g_last_error = "unexpected exception";                         \
-        return GFFT_ERR_INVALID_VALUE;                                 \
+#define GFFT_GUARD(body)                         \
+    try {                                        \
+        body;                                    \
+        return GFFT_OK;                          \
+    } catch (const Error &e) {                   \
+        g_last_error = e.msg;                    \
+        return e.status;                         \
+    } catch (const std::bad_alloc &) {           \
+        g_last_error = "host allocation failed"; \
+        return GFFT_ERR_ALLOC;                   \
+    } catch (...) {                              \
+        g_last_error = "unexpected exception";   \
+        return GFFT_ERR_INVALID_VALUE;           \
     }
 
 static gfft_plan_s *checked(gfft_plan p)
 {
     if (!p || p->magic != 0x6766u) fail(GFFT_ERR_INVALID_PLAN, "invalid plan handle");
     return p;
+}
+
+static void need_batch(long long batch)
+{
+    if (batch < 1) fail(GFFT_ERR_INVALID_SIZE, "batch must be >= 1");
+}
+
+static void need_dtype(int dtype)
+{
+    if (dtype != GFFT_F32 && dtype != GFFT_F64) fail(GFFT_ERR_INVALID_VALUE, "dtype must be GFFT_F32 or GFFT_F64");
 }
 
 extern "C" {
@@ -399,22 +447,15 @@ gfft_status gfft_plan_create(gfft_plan *plan, const gfft_desc *desc)
 
 gfft_status gfft_plan_destroy(gfft_plan plan)
 {
-    GFFT_GUARD({
-        gfft_plan_s *p = checked(plan);
-        for (int i = 0; i < 3; i++) {
-            if (p->stage[i]) cudaFree(p->stage[i]);
-            if (p->stage_out[i]) cudaFree(p->stage_out[i]);
-            if (p->host_streams[i]) cudaStreamDestroy(p->host_streams[i]);
-        }
-        if (p->ws) cudaFree(p->ws);
-        p->magic = 0;
-        delete p;
-    });
+    GFFT_GUARD({ destroy_plan(checked(plan)); });
 }
 
 gfft_status gfft_exec(gfft_plan plan, int inverse, void *out, const void *in, void *stream)
 {
-    GFFT_GUARD({ exec_plan(*checked(plan), inverse != 0, out, in, (cudaStream_t)stream); });
+    GFFT_GUARD({
+        gfft_plan_s *p = checked(plan);
+        exec_plan(*p, inverse != 0, out, in, plan_layout(*p), (cudaStream_t)stream);
+    });
 }
 
 gfft_status gfft_exec_host(gfft_plan plan, int inverse, void *out, const void *in)
@@ -430,13 +471,179 @@ gfft_status gfft_plan_launches(gfft_plan plan, int *launches)
     });
 }
 
-gfft_status gfft_fft_transform(int dtype, int n, long long batch, int inverse, void *out,
-                               const void *in, void *stream)
+gfft_status gfft_plan_workspace_size(gfft_plan plan, size_t *bytes)
 {
     GFFT_GUARD({
-        if (batch < 1) fail(GFFT_ERR_INVALID_SIZE, "batch must be >= 1");
+        if (!bytes) fail(GFFT_ERR_INVALID_VALUE, "NULL argument");
+        gfft_plan_s *p = checked(plan);
+        *bytes = p->c2c.ws_bytes + p->r2c.c2c.ws_bytes;
+    });
+}
+
+// ---- reference-shaped entry points ---------------------------------------
+
+gfft_status gfft_fft_transform(int dtype, int n, long long batch, int inverse, void *out, const void *in,
+                               void *stream)
+{
+    GFFT_GUARD({
+        need_batch(batch);
+        need_dtype(dtype);
         gfft_plan_s *p = cached_plan(GFFT_KIND_C2C, dtype, n, 0, 0);
-        exec_plan(*p, inverse != 0, out, in, (cudaStream_t)stream, batch);
+        exec_plan(*p, inverse != 0, out, in, Layout{batch, 1, n, 1, n}, (cudaStream_t)stream);
+    });
+}
+
+gfft_status gfft_fft_transform_no_scramble(int dtype, int n, long long batch, int inverse, void *inout,
+                                           void *stream)
+{
+    GFFT_GUARD({
+        need_batch(batch);
+        need_dtype(dtype);
+        gfft_plan_s *p = cached_plan(GFFT_KIND_C2C, dtype, n, 0, GFFT_FLAG_BITREV_INPUT);
+        exec_plan(*p, inverse != 0, inout, inout, Layout{batch, 1, n, 1, n}, (cudaStream_t)stream);
+    });
+}
+
+gfft_status gfft_fft_transform_real(int dtype, int n, long long batch, void *out, const void *in, void *stream)
+{
+    GFFT_GUARD({
+        need_batch(batch);
+        need_dtype(dtype);
+        gfft_plan_s *p = cached_plan(GFFT_KIND_R2C, dtype, n, 0, 0);
+        exec_plan(*p, 0, out, in, Layout{batch, 1, n, 1, n}, (cudaStream_t)stream);
+    });
+}
+
+gfft_status gfft_fft_transform_interleave(int dtype, int n, void *out, const void *in1, const void *in2,
+                                          void *stream)
+{
+    GFFT_GUARD({
+        need_dtype(dtype);
+        gfft_plan_s *p = cached_plan(GFFT_KIND_C2C, dtype, n, 0, 0);
+        check_ptr(in1, real_bytes(dtype), "in1");
+        check_ptr(in2, real_bytes(dtype), "in2");
+        check_ptr(out, cplx_bytes(dtype), "out");
+        check_cuda(launch_interleave(dtype, in1, n, in2, n, out, n, 1, n, (cudaStream_t)stream), "interleave");
+        exec_plan(*p, 0, out, out, Layout{1, 1, n, 1, n}, (cudaStream_t)stream);
+    });
+}
+
+gfft_status gfft_vert_transform(int dtype, int n, int inverse, void *out, long long out_stride, const void *in,
+                                long long in_stride, int cols, void *stream)
+{
+    GFFT_GUARD({
+        need_dtype(dtype);
+        if (cols < 1) fail(GFFT_ERR_INVALID_SIZE, "cols must be >= 1");
+        if (out == in) fail(GFFT_ERR_ALIAS, "FFTVert::transform: out must not be in (fft.h:140)");
+        if (in_stride < cols || out_stride < cols) fail(GFFT_ERR_INVALID_VALUE, "row stride below cols");
+        gfft_plan_s *p = cached_plan(GFFT_KIND_VERT, dtype, n, cols, 0);
+        exec_plan(*p, inverse != 0, out, in, Layout{1, in_stride, n * in_stride, out_stride, n * out_stride},
+                  (cudaStream_t)stream);
+    });
+}
+
+gfft_status gfft_vert_transform_no_scramble(int dtype, int n, int inverse, void *data, long long stride, int cols,
+                                            void *stream)
+{
+    GFFT_GUARD({
+        need_dtype(dtype);
+        if (cols < 1) fail(GFFT_ERR_INVALID_SIZE, "cols must be >= 1");
+        if (stride < cols) fail(GFFT_ERR_INVALID_VALUE, "row stride below cols");
+        gfft_plan_s *p = cached_plan(GFFT_KIND_VERT, dtype, n, cols, GFFT_FLAG_BITREV_INPUT);
+        exec_plan(*p, inverse != 0, data, data, Layout{1, stride, n * stride, stride, n * stride},
+                  (cudaStream_t)stream);
+    });
+}
+
+gfft_status gfft_dit_apply(int dtype, int n, void *out, const void *in, int half, void *stream)
+{
+    GFFT_GUARD({
+        need_dtype(dtype);
+        if (!is_pow2(n)) fail(GFFT_ERR_INVALID_SIZE, "size must be a power of two >= 1");
+        check_device();
+        check_ptr(in, cplx_bytes(dtype), "in");
+        check_ptr(out, cplx_bytes(dtype), "out");
+        if (n == 1) {
+            check_cuda(launch_dit_one(dtype, in, out, (cudaStream_t)stream), "DIT n=1");
+        } else {
+            const int logn = ilog2ll(n);
+            const void *dtw = cached_table("dit/" + std::to_string(dtype) + "/" + std::to_string(logn), dtype,
+                                           (size_t)n / 2 + 1,
+                                           [dtype, logn](void *buf) { dit_twiddle_fill(dtype, logn, buf); });
+            check_cuda(launch_dit(dtype, half != 0, in, out, n / 2, 1, n, n, dtw, (cudaStream_t)stream), "DIT");
+        }
+    });
+}
+
+gfft_status gfft_fft2d_transform(int dtype, int width, int height, int inverse, void *out, long long out_stride,
+                                 const void *in, long long in_stride, void *stream)
+{
+    GFFT_GUARD({
+        need_dtype(dtype);
+        gfft_plan_s *p = cached_plan(GFFT_KIND_C2C_2D, dtype, width, height, 0);
+        if (in_stride < width || out_stride < width) fail(GFFT_ERR_INVALID_VALUE, "row stride below width");
+        exec_plan(*p, inverse != 0, out, in,
+                  Layout{1, in_stride, height * in_stride, out_stride, height * out_stride}, (cudaStream_t)stream);
+    });
+}
+
+gfft_status gfft_real_fft_forward(int dtype, int n, long long batch, void *out, const void *in, int half,
+                                  void *stream)
+{
+    GFFT_GUARD({
+        need_batch(batch);
+        need_dtype(dtype);
+        gfft_plan_s *p = cached_plan(GFFT_KIND_R2C, dtype, n, 0, half ? GFFT_FLAG_HALF_SPECTRUM : 0);
+        // the reference's output buffer holds n complex values either way
+        exec_plan(*p, 0, out, in, Layout{batch, 1, n, 1, n}, (cudaStream_t)stream);
+    });
+}
+
+gfft_status gfft_real_fft2d_forward(int dtype, int width, int height, void *out, long long out_stride,
+                                    const void *in, long long in_stride, void *stream)
+{
+    GFFT_GUARD({
+        need_dtype(dtype);
+        if (width > 1 && (in_stride % 2)) fail(GFFT_ERR_INVALID_VALUE, "input row stride must be even");
+        if (in_stride < width || out_stride < width) fail(GFFT_ERR_INVALID_VALUE, "row stride below width");
+        gfft_plan_s *p = cached_plan(GFFT_KIND_R2C_2D, dtype, width, height, 0);
+        exec_plan(*p, 0, out, in, Layout{1, in_stride, height * in_stride, out_stride, height * out_stride},
+                  (cudaStream_t)stream);
+    });
+}
+
+gfft_status gfft_real_fft2d_forward_2x(int dtype, int width, int height, void *out, long long out_stride,
+                                       const void *in1, long long in_stride1, const void *in2,
+                                       long long in_stride2, void *stream)
+{
+    GFFT_GUARD({
+        need_dtype(dtype);
+        if (out_stride < width || in_stride1 < width || in_stride2 < width)
+            fail(GFFT_ERR_INVALID_VALUE, "row stride below width");
+        gfft_plan_s *p = cached_plan(GFFT_KIND_C2C_2D, dtype, width, height, 0);
+        check_ptr(in1, real_bytes(dtype), "in1");
+        check_ptr(in2, real_bytes(dtype), "in2");
+        check_ptr(out, cplx_bytes(dtype), "out");
+        // rows hold in1 + i in2, then the complex 2D transform in place
+        check_cuda(launch_interleave(dtype, in1, in_stride1, in2, in_stride2, out, out_stride, height, width,
+                                     (cudaStream_t)stream),
+                   "interleave");
+        exec_plan(*p, 0, out, out, Layout{1, out_stride, height * out_stride, out_stride, height * out_stride},
+                  (cudaStream_t)stream);
+    });
+}
+
+gfft_status gfft_separate_2x_real_fft(int dtype, int n, void *out1, void *out2, const void *in, void *stream)
+{
+    GFFT_GUARD({
+        need_dtype(dtype);
+        if (!is_pow2(n) || n < 2) fail(GFFT_ERR_INVALID_SIZE, "size must be a power of two >= 2");
+        check_device();
+        check_ptr(in, cplx_bytes(dtype), "in");
+        check_ptr(out1, cplx_bytes(dtype), "out1");
+        check_ptr(out2, cplx_bytes(dtype), "out2");
+        if (out1 == out2) fail(GFFT_ERR_ALIAS, "out1 and out2 must differ");
+        check_cuda(launch_separate2x(dtype, in, out1, out2, n, (cudaStream_t)stream), "separate");
     });
 }
 

@@ -1,0 +1,194 @@
+// plan.cpp -- transform cores (C2C, column, real-input) and their launch
+// sequences.  All device work is stream-ordered on the caller's stream.
+#include <algorithm>
+#include <cstdlib>
+#include <string>
+
+#include "plan.h"
+#include "twiddle.h"
+
+namespace gfft {
+
+bool is_pow2(long long n) { return n > 0 && (n & (n - 1)) == 0; }
+int ilog2ll(long long n)
+{
+    int l = 0;
+    while ((1LL << l) < n) l++;
+    return l;
+}
+size_t cplx_bytes(int dtype) { return dtype == GFFT_F64 ? 16 : 8; }
+
+static long long env_ll(const char *name, long long dflt)
+{
+    const char *v = std::getenv(name);
+    return (v && *v) ? std::atoll(v) : dflt;
+}
+
+static const void *tile_table(int dtype, const TileKernel *k, int logl, int c)
+{
+    return cached_table("tile/" + std::to_string(dtype) + "/" + std::to_string(logl) + "/" + std::to_string(c) +
+                            "/" + std::to_string(k->threads),
+                        dtype, k->twcount, [k](void *buf) { k->fill(buf); });
+}
+
+// ---------------------------------------------------------------------------
+// C2C
+
+void C2CCore::init(int dtype_, int logn_, long long batch_hint)
+{
+    dtype = dtype_;
+    logn = logn_;
+    if (logn <= fused_max_logn(dtype)) {
+        algo = 1;
+        const int d = dtype, l = logn;
+        tw = cached_table("fused/" + std::to_string(d) + "/" + std::to_string(l), d, fused_twiddle_count(d, l),
+                          [d, l](void *buf) { fused_twiddle_fill(d, l, buf); });
+        return;
+    }
+    if (logn > 24) fail(GFFT_ERR_INVALID_SIZE, "transform length above 2^24 is not supported");
+    // N = A * B, A = column-FFT length, B = row-FFT length, both <= 2^12
+    logA = logn / 2;
+    logB = logn - logA;
+    const int maxc = (int)env_ll("GFFT_TILE_MAXC", 16);
+    ccol = tile_widest(dtype, TILE_COL_TW4, logA, maxc);
+    crow = tile_widest(dtype, TILE_ROW_XPOSE, logB, maxc);
+    if (!ccol || !crow) fail(GFFT_ERR_UNSUPPORTED, "no tile kernel for this length");
+    kcol = tile_find(dtype, TILE_COL_TW4, logA, ccol);
+    krow = tile_find(dtype, TILE_ROW_XPOSE, logB, crow);
+    tw_col = tile_table(dtype, kcol, logA, ccol);
+    tw_row = tile_table(dtype, krow, logB, crow);
+    // inter-pass twiddle W_N^e = tw_hi[e >> lo_bits] * tw_lo[e & (2^lo_bits - 1)]
+    lo_bits = (logn + 1) / 2;
+    const long long N = 1LL << logn;
+    const int d = dtype;
+    auto fill = [d, N](long long count, long long mul) {
+        return [d, N, count, mul](void *buf) {
+            for (long long e = 0; e < count; e++) {
+                if (d == GFFT_F32) forward_root<float>(e * mul, N, &((float *)buf)[2 * e], &((float *)buf)[2 * e + 1]);
+                else forward_root<double>(e * mul, N, &((double *)buf)[2 * e], &((double *)buf)[2 * e + 1]);
+            }
+        };
+    };
+    const std::string key = "4s/" + std::to_string(dtype) + "/" + std::to_string(logn);
+    tw_lo = cached_table(key + "/lo", dtype, 1LL << lo_bits, fill(1LL << lo_bits, 1));
+    tw_hi = cached_table(key + "/hi", dtype, N >> lo_bits, fill(N >> lo_bits, 1LL << lo_bits));
+    // transforms per launch pair, bounded by the workspace budget
+    const long long budget = env_ll("GFFT_WS_BUDGET_MB", 512) << 20;
+    group = std::max<long long>(1, budget / (N * (long long)cplx_bytes(dtype)));
+    group = std::min(group, std::max<long long>(1, batch_hint));
+    ws_bytes = (size_t)(group * N) * cplx_bytes(dtype);
+    check_cuda(cudaMalloc(&ws, ws_bytes), "cudaMalloc(workspace)");
+    algo = 2;
+}
+
+void C2CCore::release()
+{
+    if (ws) cudaFree(ws);
+    ws = nullptr;
+}
+
+int C2CCore::launches(long long batch) const
+{
+    if (algo == 1) return 1;
+    return 2 * (int)((batch + group - 1) / group);
+}
+
+void C2CCore::run(int inverse, const void *in, void *out, long long batch, long long idist, long long odist,
+                  long long istride, long long ostride, cudaStream_t st) const
+{
+    if (algo == 1) {
+        FusedC2CArgs a{in, out, batch, idist, odist, istride, ostride, tw};
+        check_cuda(launch_fused_c2c(dtype, logn, inverse, a, st), "launch fused C2C");
+        return;
+    }
+    if (istride != 1 || ostride != 1)
+        fail(GFFT_ERR_UNSUPPORTED, "lengths above the fused limit need unit element strides");
+    const long long A = 1LL << logA, B = 1LL << logB, N = A * B;
+    const size_t eb = cplx_bytes(dtype);
+    const unsigned nmask = (unsigned)(N - 1);
+    for (long long g0 = 0; g0 < batch; g0 += group) {
+        const long long nb = std::min(group, batch - g0);
+        const char *src = static_cast<const char *>(in) + (size_t)(g0 * idist) * eb;
+        char *dst = static_cast<char *>(out) + (size_t)(g0 * odist) * eb;
+        // column pass: B columns of A points (row stride B) into the workspace
+        check_cuda(launch_colpass(*kcol, inverse, B / ccol, nb, src, ws, B, B, B, idist, N, tw_col, tw_lo, tw_hi,
+                                  lo_bits, nmask, st),
+                   "launch column pass");
+        // row pass: A rows of B points, stored transposed (stride A)
+        check_cuda(launch_rowpass(*krow, inverse, A / crow, nb, ws, dst, A, B, A, N, odist, tw_row, st),
+                   "launch row pass");
+    }
+}
+
+// ---------------------------------------------------------------------------
+// column FFTs
+
+void ColCore::init(int dtype_, int logl_, int variant_)
+{
+    dtype = dtype_;
+    logl = logl_;
+    variant = variant_;
+    if (logl > 12) fail(GFFT_ERR_UNSUPPORTED, "column length above 2^12 is not supported");
+    c = tile_widest(dtype, variant, logl, (int)env_ll("GFFT_COL_MAXC", 16));
+    if (!c) fail(GFFT_ERR_UNSUPPORTED, "no column kernel for this length");
+    k = tile_find(dtype, variant, logl, c);
+    tw = tile_table(dtype, k, logl, c);
+}
+
+void ColCore::run(int inverse, const void *in, void *out, long long ncols, long long ld_in, long long ld_out,
+                  long long batch, long long idist, long long odist, cudaStream_t st) const
+{
+    check_cuda(launch_colpass(*k, inverse, (ncols + c - 1) / c, batch, in, out, ncols, ld_in, ld_out, idist, odist,
+                              tw, nullptr, nullptr, 0, 0u, st),
+               "launch column FFT");
+}
+
+// ---------------------------------------------------------------------------
+// real input
+
+void R2CCore::init(int dtype_, int logn_, int half_, long long batch_hint)
+{
+    dtype = dtype_;
+    logn = logn_;
+    half = half_;
+    if (logn == 0) {
+        algo = 0;
+        return;
+    }
+    const int d = dtype, l = logn, lh = logn - 1;
+    dtw = cached_table("dit/" + std::to_string(d) + "/" + std::to_string(l), d, (1LL << lh) + 1,
+                       [d, l](void *buf) { dit_twiddle_fill(d, l, buf); });
+    if (lh <= r2c_fused_max_logh(dtype)) {
+        algo = 1;
+        tw = cached_table("r2c/" + std::to_string(d) + "/" + std::to_string(lh), d, r2c_twiddle_count(d, lh),
+                          [d, lh](void *buf) { r2c_twiddle_fill(d, lh, buf); });
+        return;
+    }
+    algo = 2;
+    c2c.init(dtype, lh, batch_hint);
+}
+
+int R2CCore::launches(long long batch) const
+{
+    if (algo == 2) return c2c.launches(batch) + 1;
+    return 1;
+}
+
+void R2CCore::run(const void *in, void *out, long long batch, long long idist, long long odist,
+                  cudaStream_t st) const
+{
+    if (algo == 0) {
+        check_cuda(launch_r2c_one(dtype, in, out, batch, idist, odist, st), "launch R2C n=1");
+    } else if (algo == 1) {
+        check_cuda(launch_r2c_fused(dtype, logn - 1, half, in, out, batch, idist, odist, tw, dtw, st),
+                   "launch fused R2C");
+    } else {
+        const long long H = 1LL << (logn - 1);
+        // n reals are n/2 complex; transform them into the output buffer,
+        // then adjust in place (the reference's order, FFTReal.h:209-211)
+        c2c.run(0, in, out, batch, idist / 2, odist, 1, 1, st);
+        check_cuda(launch_dit(dtype, half, out, out, H, batch, odist, odist, dtw, st), "launch DIT pass");
+    }
+}
+
+}  // namespace gfft

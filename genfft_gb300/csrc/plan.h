@@ -1,0 +1,96 @@
+// plan.h -- internal plan objects: reusable transform "cores" and the plan
+// that strings them together per gfft_kind.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <mutex>
+
+#include "internal.h"
+#include "tiles_registry.h"
+
+namespace gfft {
+
+size_t cplx_bytes(int dtype);
+int ilog2ll(long long n);
+bool is_pow2(long long n);
+
+// Batched 1D C2C of n = 2^logn points: one fused kernel up to the shared
+// memory limit, else the four-step column + row passes through a workspace.
+struct C2CCore {
+    int dtype = 0, logn = 0;
+    int algo = 0;  // 1 fused, 2 four-step
+    const void *tw = nullptr;
+    int logA = 0, logB = 0, ccol = 0, crow = 0, lo_bits = 0;
+    const TileKernel *kcol = nullptr, *krow = nullptr;
+    const void *tw_col = nullptr, *tw_row = nullptr, *tw_lo = nullptr, *tw_hi = nullptr;
+    long long group = 0;       // transforms per column/row launch pair
+    void *ws = nullptr;        // group * n elements
+    size_t ws_bytes = 0;
+
+    void init(int dtype, int logn, long long batch_hint);
+    void release();
+    int launches(long long batch) const;
+    // strides in complex elements; four-step needs unit element strides
+    void run(int inverse, const void *in, void *out, long long batch, long long idist, long long odist,
+             long long istride, long long ostride, cudaStream_t st) const;
+};
+
+// Column FFTs of length 2^logl over ncols columns (tile kernels).
+struct ColCore {
+    int dtype = 0, logl = 0, variant = 0, c = 0;
+    const TileKernel *k = nullptr;
+    const void *tw = nullptr;
+    void init(int dtype, int logl, int variant);
+    void run(int inverse, const void *in, void *out, long long ncols, long long ld_in, long long ld_out,
+             long long batch, long long idist, long long odist, cudaStream_t st) const;
+};
+
+// Real-input 1D transform of n = 2^logn reals (RealFFT<T>::forward).
+struct R2CCore {
+    int dtype = 0, logn = 0, half = 1;
+    int algo = 0;  // 0 n == 1, 1 fused, 2 C2C(n/2) + DIT pass
+    const void *tw = nullptr, *dtw = nullptr;
+    C2CCore c2c;
+    void init(int dtype, int logn, int half, long long batch_hint);
+    void release() { c2c.release(); }
+    int launches(long long batch) const;
+    // idist in reals (even), odist in complex elements
+    void run(const void *in, void *out, long long batch, long long idist, long long odist, cudaStream_t st) const;
+};
+
+// ---- kernels in real.cu --------------------------------------------------
+int r2c_fused_max_logh(int dtype);
+size_t r2c_twiddle_count(int dtype, int logh);
+void r2c_twiddle_fill(int dtype, int logh, void *buf);
+void dit_twiddle_fill(int dtype, int logn, void *buf);
+cudaError_t launch_r2c_fused(int dtype, int logh, int half, const void *in, void *out, long long batch,
+                             long long idist, long long odist, const void *tw, const void *dtw, cudaStream_t st);
+cudaError_t launch_dit(int dtype, int half, const void *in, void *out, long long H, long long batch,
+                       long long idist, long long odist, const void *dtw, cudaStream_t st);
+cudaError_t launch_dit_one(int dtype, const void *in, void *out, cudaStream_t st);
+cudaError_t launch_r2c_one(int dtype, const void *in, void *out, long long batch, long long idist, long long odist,
+                           cudaStream_t st);
+cudaError_t launch_separate2x(int dtype, const void *in, void *o1, void *o2, long long n, cudaStream_t st);
+cudaError_t launch_interleave(int dtype, const void *a, long long lda, const void *b, long long ldb, void *z,
+                              long long ldz, long long rows, long long cols, cudaStream_t st);
+cudaError_t launch_bitrev_swap(int dtype, void *x, int logn, long long batch, long long dist, cudaStream_t st);
+
+}  // namespace gfft
+
+// the public handle
+struct gfft_plan_s {
+    gfft_desc d;
+    unsigned magic = 0x6766u;
+    int device = 0;
+    int launches = 0;
+    gfft::C2CCore c2c;   // C2C; 2D row pass
+    gfft::ColCore col;   // 2D column pass; VERT
+    gfft::R2CCore r2c;   // R2C; real-2D row pass
+    // host-path staging (owned, lazily allocated)
+    std::mutex host_mu;
+    void *stage[3] = {nullptr, nullptr, nullptr};
+    void *stage_out[3] = {nullptr, nullptr, nullptr};
+    size_t stage_bytes_in = 0, stage_bytes_out = 0;
+    cudaStream_t host_streams[3] = {nullptr, nullptr, nullptr};
+};

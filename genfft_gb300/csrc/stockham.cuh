@@ -28,6 +28,13 @@ __device__ __forceinline__ int spad(int i)
     return sizeof(T) == 4 ? i + (i >> 4) : i + (i >> 3);
 }
 
+// padded slot count for n elements laid out through spad<T>
+template <typename T>
+__host__ __device__ constexpr int spad_size(int n)
+{
+    return n <= 1 ? 1 : n + (sizeof(T) == 4 ? n / 16 : n / 8) + 1;
+}
+
 template <typename T, int LOGN, int E_>
 struct StockhamPlan {
     static constexpr int N = 1 << LOGN;

@@ -16,13 +16,6 @@
 
 namespace gfft {
 
-// padded slot count for n elements laid out through spad<T>
-template <typename T>
-__host__ __device__ constexpr int spad_size(int n)
-{
-    return n <= 1 ? 1 : n + (sizeof(T) == 4 ? n / 16 : n / 8) + 1;
-}
-
 // Column-major tile layout: column s occupies PITCH slots starting at
 // s*PITCH and is addressed like a fused transform (spad).  PITCH is chosen
 // so that the C columns a half-warp (fp32) or quarter-warp (fp64) touches
@@ -52,9 +45,12 @@ struct ColCfg {
 // and its transform goes to out[b*odist + i*ld_out + col], multiplied by
 // W_N^(col*i) when TW4 (four-step inter-pass twiddle, from the split tables
 // tw_hi[e >> lo_bits] * tw_lo[e & lo_mask], e = col*i mod N).
+// HERM (real 2D output, RealFFT2D::forward, FFTReal.h:90-103): the tile runs
+// over the W/2+1 non-redundant columns (ncols = W/2+1) and also stores the
+// Hermitian mirror X[(L-i) mod L][W-col] = conj X[i][col] for 0 < col < W/2.
 // Threads are numbered t*C + s, so a warp touches C consecutive columns of
 // a row and global accesses come in C-element runs.
-template <typename T, int LOGL, int C, int E_, bool INV, bool TW4, bool BITREV>
+template <typename T, int LOGL, int C, int E_, bool INV, bool TW4, bool BITREV, bool HERM = false>
 __global__ void __launch_bounds__(ColCfg<T, LOGL, C, E_>::THREADS)
     k_colpass(const cpx<T> *__restrict__ in, cpx<T> *__restrict__ out, long long ncols, long long ld_in,
               long long ld_out, long long idist, long long odist,
@@ -110,6 +106,17 @@ __global__ void __launch_bounds__(ColCfg<T, LOGL, C, E_>::THREADS)
                     if ((q & 3) == 3) asm volatile("" ::: "memory");
                 }
                 st_c(dst, val);
+            }
+            if constexpr (HERM) {
+                const long long W = 2 * (ncols - 1);
+                if (col > 0 && 2 * col < W) {
+                    cpx<T> *mir = out + b * odist + (W - col);
+#pragma unroll
+                    for (int q = 0; q < E; q++) {
+                        const int i = t + q * G;
+                        st_c(mir + (long long)((SP::N - i) & (SP::N - 1)) * ld_out, conj(v[q]));
+                    }
+                }
             }
         }
     }

@@ -30,9 +30,9 @@ struct TileReg {
             k.smem = Cfg::SMEM;
         } else {
             using Cfg = ColCfg<T, LOGL, C, E>;
-            constexpr bool tw4 = V == TILE_COL_TW4, br = V == TILE_COL_BITREV;
-            k.fwd = (const void *)&k_colpass<T, LOGL, C, E, false, tw4, br>;
-            k.inv = (const void *)&k_colpass<T, LOGL, C, E, true, tw4, br>;
+            constexpr bool tw4 = V == TILE_COL_TW4, br = V == TILE_COL_BITREV, herm = V == TILE_COL_HERM;
+            k.fwd = (const void *)&k_colpass<T, LOGL, C, E, false, tw4, br, herm>;
+            k.inv = (const void *)&k_colpass<T, LOGL, C, E, true, tw4, br, herm>;
             k.threads = Cfg::THREADS;
             k.smem = Cfg::SMEM;
         }

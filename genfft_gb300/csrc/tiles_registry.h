@@ -13,7 +13,8 @@ enum TileVariant {
     TILE_COL_TW4 = 0,     // column pass of the four-step split (with W_N twiddle)
     TILE_COL_PLAIN = 1,   // column FFT, natural-order input
     TILE_COL_BITREV = 2,  // column FFT, bit-reversed row order on input
-    TILE_ROW_XPOSE = 3    // row pass with transposed store
+    TILE_ROW_XPOSE = 3,   // row pass with transposed store
+    TILE_COL_HERM = 4     // column FFT + Hermitian mirror store (real 2D)
 };
 
 struct TileKernel {

@@ -94,6 +94,8 @@ gfft_status gfft_exec(gfft_plan plan, int inverse, void *out, const void *in, vo
 gfft_status gfft_exec_host(gfft_plan plan, int inverse, void *out, const void *in);
 /* number of kernel launches one gfft_exec makes (for launch accounting) */
 gfft_status gfft_plan_launches(gfft_plan plan, int *launches);
+/* device workspace the plan owns (bytes; 0 for single-kernel sizes) */
+gfft_status gfft_plan_workspace_size(gfft_plan plan, size_t *bytes);
 
 /* ---- reference-shaped entry points (device pointers) ------------------ */
 /* Each mirrors one call of the reference C++ API; plans are cached per
@@ -104,6 +106,54 @@ gfft_status gfft_plan_launches(gfft_plan plan, int *launches);
  * (fft.h:80-85).  out != in is not required here (in-place is allowed). */
 gfft_status gfft_fft_transform(int dtype, int n, long long batch, int inverse, void *out,
                                const void *in, void *stream);
+/* FFT<T>(n).transform_no_scramble<inverse>(inout): in place, bit-reversed
+ * input, natural-order output (fft.h:69-73). */
+gfft_status gfft_fft_transform_no_scramble(int dtype, int n, long long batch, int inverse,
+                                           void *inout, void *stream);
+/* FFT<T>(n).transform_real(out, in): n reals -> n complex bins (fft.h:90-94) */
+gfft_status gfft_fft_transform_real(int dtype, int n, long long batch, void *out, const void *in,
+                                    void *stream);
+/* FFT<T>(n).transform_interleave(out, in1, in2): FFT of in1 + i*in2,
+ * separate with gfft_separate_2x_real_fft (fft.h:100-105) */
+gfft_status gfft_fft_transform_interleave(int dtype, int n, void *out, const void *in1,
+                                          const void *in2, void *stream);
+/* FFTVert<T>(n).transform<inverse>(out, out_stride, in, in_stride, cols):
+ * length-n FFT down each of `cols` columns; strides in complex elements;
+ * out must not be in (fft.h:145-150). */
+gfft_status gfft_vert_transform(int dtype, int n, int inverse, void *out, long long out_stride,
+                                const void *in, long long in_stride, int cols, void *stream);
+/* FFTVert<T>(n).transform_no_scramble<inverse>(data, stride, cols): in
+ * place, rows in bit-reversed order (fft.h:132-136). */
+gfft_status gfft_vert_transform_no_scramble(int dtype, int n, int inverse, void *data,
+                                            long long stride, int cols, void *stream);
+/* DIT<T>(n).apply(out, in, half): real-FFT adjustment of the n/2-point
+ * complex FFT `in` into the spectrum `out` (n/2+1 bins if half, else n);
+ * out may equal in (fft.h:180-188, fft_dit_impl_generic.inl:27-61). */
+gfft_status gfft_dit_apply(int dtype, int n, void *out, const void *in, int half, void *stream);
+/* FFT2D<T>(width, height).transform<inverse>(out, out_stride, in, in_stride):
+ * row-major [height][width], strides in complex elements (fft.h:213-218). */
+gfft_status gfft_fft2d_transform(int dtype, int width, int height, int inverse, void *out,
+                                 long long out_stride, const void *in, long long in_stride,
+                                 void *stream);
+/* RealFFT<T>(n).forward(out, in, half) over `batch` transforms: n reals in,
+ * n/2+1 (half) or n bins out; transforms are n reals / n complex apart like
+ * the reference's buffers (FFTReal.h:204-213). */
+gfft_status gfft_real_fft_forward(int dtype, int n, long long batch, void *out, const void *in,
+                                  int half, void *stream);
+/* RealFFT2D<T>(width, height).forward(out, out_stride, in, in_stride):
+ * full-width Hermitian output; in_stride in reals, out_stride in complex
+ * elements (FFTReal.h:83-104). */
+gfft_status gfft_real_fft2d_forward(int dtype, int width, int height, void *out, long long out_stride,
+                                    const void *in, long long in_stride, void *stream);
+/* RealFFT2D<T>(width, height).forward_2x: 2D FFT of in1 + i*in2
+ * (FFTReal.h:114-118) */
+gfft_status gfft_real_fft2d_forward_2x(int dtype, int width, int height, void *out,
+                                       long long out_stride, const void *in1, long long in_stride1,
+                                       const void *in2, long long in_stride2, void *stream);
+/* separate_2x_real_FFT(out1, out2, in, n); out1 or out2 may be in
+ * (FFTReal.h:34-66) */
+gfft_status gfft_separate_2x_real_fft(int dtype, int n, void *out1, void *out2, const void *in,
+                                      void *stream);
 
 const char *gfft_status_string(gfft_status status);
 /* message of the last failed call on this thread ("" if none) */
