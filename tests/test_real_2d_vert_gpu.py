@@ -223,7 +223,7 @@ def test_real_fft2d_4096(gfft, oracle):
     assert close(full[:, :2049], half, 0)
     # Hermitian fill: X[k][W-j] = conj X[(H-k) % H][j]
     k = np.arange(4096)
-    assert close(full[:, 2049:], np.conj(half[(-k) % 4096][:, 1:2047][:, ::-1]), 0)
+    assert close(full[:, 2049:], np.conj(half[(-k) % 4096][:, 1:2048][:, ::-1]), 0)
 
 
 def test_2d_batched_strided_fp64(gfft):
@@ -246,8 +246,9 @@ def test_alias_errors(gfft):
     with pytest.raises(gfft.GFFTError) as e:
         gfft._check(gfft.lib().gfft_real_fft_forward(0, 64, 1, xr.data_ptr(), xr.data_ptr(), 1, 0))
     assert e.value.name == "GFFT_ERR_ALIAS"
+    # the real-input transform has no inverse (FFTReal.h:186-221)
+    p = gfft.Plan(gfft.KIND_R2C, gfft.F32, 64, 0, 1)
+    out = torch.zeros(64, dtype=torch.complex64, device="cuda")
     with pytest.raises(gfft.GFFTError) as e:
-        gfft.rfft2(torch.zeros(64, 64, dtype=torch.float32, device="cuda"), half=True) and None
-        p = gfft.Plan(gfft.KIND_R2C, gfft.F32, 64, 0, 1)
-        p.exec_ptr(xr.data_ptr(), xr.data_ptr(), True, 0)
-    assert e.value.name in ("GFFT_ERR_UNSUPPORTED", "GFFT_ERR_ALIAS")
+        p.exec_ptr(out.data_ptr(), xr.data_ptr(), True, 0)
+    assert e.value.name == "GFFT_ERR_UNSUPPORTED"
