@@ -33,13 +33,17 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-# name -> (kind, dtype, n0, n1, batch)
+# name -> (kind, dtype, n0, n1, batch); 2D kinds: n0 = width, n1 = height
 WORKLOADS = {
     "c2c_f32_4096x16384": ("c2c", "f32", 1 << 12, 0, 16384),
     "c2c_f32_1024x65536": ("c2c", "f32", 1 << 10, 0, 65536),
     "c2c_f64_4096x8192": ("c2c", "f64", 1 << 12, 0, 8192),
     "c2c_f32_4194304x32": ("c2c", "f32", 1 << 22, 0, 32),
     "c2c_f64_65536x512": ("c2c", "f64", 1 << 16, 0, 512),
+    "c2c_f32_65536x4096": ("c2c", "f32", 1 << 16, 0, 4096),
+    "r2c_f32_1048576x64": ("r2c", "f32", 1 << 20, 0, 64),
+    "c2d_f32_4096x4096": ("c2d", "f32", 4096, 4096, 1),
+    "r2d_f32_4096x4096": ("r2d", "f32", 4096, 4096, 1),
 }
 DEFAULT = "c2c_f32_4096x16384"
 
@@ -59,11 +63,31 @@ def elem_bytes(dtype):
 
 
 def algo_bytes_per_transform(kind, dtype, n0, n1):
-    return 2 * n0 * elem_bytes(dtype)
+    """Read the input once + write the output once (real in/out counted as
+    reals; real outputs are the n/2+1 half spectrum)."""
+    cb, rb = elem_bytes(dtype), elem_bytes(dtype) // 2
+    if kind == "c2c":
+        return 2 * n0 * cb
+    if kind == "r2c":
+        return n0 * rb + (n0 // 2 + 1) * cb
+    if kind == "c2d":
+        return 2 * n0 * n1 * cb
+    if kind == "r2d":
+        return n0 * n1 * rb + (n0 // 2 + 1) * n1 * cb
+    raise ValueError(kind)
 
 
 def flops_per_transform(kind, n0, n1):
-    return 5.0 * n0 * math.log2(n0) if n0 > 1 else 0.0
+    """5 N log2 N for complex transforms; 2.5 N log2 N for real input."""
+    n = n0 * (n1 if kind in ("c2d", "r2d") else 1)
+    f = 5.0 * n * math.log2(n) if n > 1 else 0.0
+    return f / 2 if kind in ("r2c", "r2d") else f
+
+
+def execs_per_step(kind):
+    """forward + unscaled inverse for complex kinds; forward only for real
+    input (the reference has no real inverse, FFTReal.h:127-130)."""
+    return 2 if kind in ("c2c", "c2d") else 1
 
 
 def measured_peak():
@@ -202,30 +226,53 @@ def cpu_impl():
 
 
 def time_cpu(kind, dtype, n0, n1, batch, budget_s=8.0, max_reps=20):
+    """Time the reference algorithm on the host cores over the full batch
+    (C2C, R2C) or one 2D transform; returns (cpu_baseline dict, median
+    seconds per step, steps timed)."""
     import numpy as np
     L, prefix, kindname = cpu_impl()
     cores = os.cpu_count() or 1
     rng = np.random.default_rng(0)
     cdt = np.complex64 if dtype == "f32" else np.complex128
-    x = (rng.standard_normal((batch, n0)) + 1j * rng.standard_normal((batch, n0))).astype(cdt)
-    y = np.empty_like(x)
-    z = np.empty_like(x)
-    fn = getattr(L, f"{prefix}fft_batch_{dtype[0]}")
+    rdt = np.float32 if dtype == "f32" else np.float64
     p = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
-    # one untimed warm-up step (page faults, plan creation)
-    fn(p(y), p(x), n0, batch, 0, cores)
+    s = dtype[0]
+    if kind == "c2c":
+        x = (rng.standard_normal((batch, n0)) + 1j * rng.standard_normal((batch, n0))).astype(cdt)
+        y, z = np.empty_like(x), np.empty_like(x)
+        fn = getattr(L, f"{prefix}fft_batch_{s}")
+        run = lambda: (fn(p(y), p(x), n0, batch, 0, cores), fn(p(z), p(y), n0, batch, 1, cores))  # noqa: E731
+        desc, threads = f"forward+inverse of the full {batch} x {n0} batch", cores
+    elif kind == "r2c":
+        x = rng.uniform(-1, 1, (batch, n0)).astype(rdt)
+        y = np.empty((batch, n0), dtype=cdt)
+        fn = getattr(L, f"{prefix}real_fft_batch_f")
+        run = lambda: fn(p(y), n0, p(x), n0, n0, batch, 1, cores)  # noqa: E731
+        desc, threads = f"half-spectrum forward of the full {batch} x {n0} batch", cores
+    elif kind == "c2d":
+        x = (rng.uniform(-1, 1, (n1, n0)) + 1j * rng.uniform(-1, 1, (n1, n0))).astype(cdt)
+        y, z = np.empty_like(x), np.empty_like(x)
+        fn = getattr(L, f"{prefix}fft2d_{s}")
+        run = lambda: (fn(p(y), n0, p(x), n0, n0, n1, 0), fn(p(z), n0, p(y), n0, n0, n1, 1))  # noqa: E731
+        desc, threads = f"forward+inverse of one {n1} x {n0} transform (single-threaded API)", 1
+    else:
+        x = rng.uniform(-1, 1, (n1, n0)).astype(rdt)
+        y = np.empty((n1, n0), dtype=cdt)
+        fn = getattr(L, f"{prefix}real_fft2d_{s}")
+        run = lambda: fn(p(y), n0, p(x), n0, n0, n1)  # noqa: E731
+        desc, threads = f"forward of one {n1} x {n0} real transform, full width (single-threaded API)", 1
+    run()  # untimed warm-up (page faults, plan creation)
     times = []
     t_start = time.perf_counter()
     while len(times) < max_reps and (time.perf_counter() - t_start) < budget_s:
         t0 = time.perf_counter()
-        fn(p(y), p(x), n0, batch, 0, cores)
-        fn(p(z), p(y), n0, batch, 1, cores)
+        run()
         times.append(time.perf_counter() - t0)
-    step_bytes = 2 * batch * algo_bytes_per_transform(kind, dtype, n0, n1)
+    nb = batch if kind in ("c2c", "r2c") else 1
+    step_bytes = execs_per_step(kind) * nb * algo_bytes_per_transform(kind, dtype, n0, n1)
     med = statistics.median(times)
-    return {"value": step_bytes / med / 1e9, "unit": "GB/s", "cores": cores, "kind": kindname,
-            "sample": f"{len(times)} steps (forward+inverse) of the full {batch} x {n0} batch, "
-                      f"{cores} threads, median step {med * 1e3:.1f} ms"}, med, len(times)
+    return {"value": step_bytes / med / 1e9, "unit": "GB/s", "cores": threads, "kind": kindname,
+            "sample": f"{len(times)} steps ({desc}), {threads} threads, median step {med * 1e3:.1f} ms"}, med, len(times)
 
 
 # ---------------------------------------------------------------------------
@@ -273,7 +320,8 @@ def run_reference(args):
         "unit": "GB/s", "n_gpus": args.gpus, "steps": reps, "warmup": 1,
         "ms_per_step": round(med * 1e3, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": dtype, "data": "synthetic",
-        "config": {"workload": args.workload, "n": n0, "batch": batch, "step": "forward+inverse",
+        "config": {"workload": args.workload, "n": n0, "height": n1 or None, "batch": batch,
+                   "step": "forward+inverse" if execs_per_step(kind) == 2 else "forward",
                    "threads": cb["cores"]},
         "cpu_baseline": cb,
         "e2e": {"value": round(cb["value"], 3), "unit": "GB/s", "h2d_bytes_per_step": 0,
@@ -281,6 +329,34 @@ def run_reference(args):
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def make_case(G, torch, kind, dtype, n0, n1, batch, rank):
+    """Inputs, outputs, plan and the per-step exec list for one workload."""
+    rdt = torch.float32 if dtype == "f32" else torch.float64
+    cdt = torch.complex64 if dtype == "f32" else torch.complex128
+    dcode = G.F32 if dtype == "f32" else G.F64
+    gen = torch.Generator(device="cuda").manual_seed(1234 + rank)
+    if kind == "c2c":
+        shape_in = shape_out = (batch, n0)
+        x = torch.randn(*shape_in, dtype=cdt, device="cuda", generator=gen)
+        plan = G.Plan(G.KIND_C2C, dcode, n0, 0, batch)
+    elif kind == "c2d":
+        shape_in = shape_out = (batch, n1, n0)
+        x = torch.rand(*shape_in, dtype=cdt, device="cuda", generator=gen) * 2 - (1 + 1j)
+        plan = G.Plan(G.KIND_C2C_2D, dcode, n0, n1, batch)
+    elif kind == "r2c":
+        shape_in, shape_out = (batch, n0), (batch, n0 // 2 + 1)
+        x = torch.rand(*shape_in, dtype=rdt, device="cuda", generator=gen) * 2 - 1
+        plan = G.Plan(G.KIND_R2C, dcode, n0, 0, batch, G.FLAG_HALF_SPECTRUM)
+    else:  # r2d
+        shape_in, shape_out = (batch, n1, n0), (batch, n1, n0 // 2 + 1)
+        x = torch.rand(*shape_in, dtype=rdt, device="cuda", generator=gen) * 2 - 1
+        plan = G.Plan(G.KIND_R2C_2D, dcode, n0, n1, batch, G.FLAG_HALF_SPECTRUM)
+    y = torch.empty(*shape_out, dtype=cdt, device="cuda")
+    z = torch.empty_like(x) if kind in ("c2c", "c2d") else None
+    execs = [(y, x, False)] + ([(z, y, True)] if z is not None else [])
+    return x, y, z, plan, execs
 
 
 def run_ours(args):
@@ -293,22 +369,15 @@ def run_ours(args):
     dev = local if world > 1 else 0
     torch.cuda.set_device(dev)
     kind, dtype, n0, n1, batch = WORKLOADS[args.workload]
-    cdt = torch.complex64 if dtype == "f32" else torch.complex128
-    dcode = G.F32 if dtype == "f32" else G.F64
     G.lib()
-
-    gen = torch.Generator(device="cuda").manual_seed(1234 + rank)
-    x = torch.randn(batch, n0, dtype=cdt, device="cuda", generator=gen)
-    y = torch.empty_like(x)
-    z = torch.empty_like(x)
-    plan = G.Plan(G.KIND_C2C, dcode, n0, 0, batch)
+    x, y, z, plan, execs = make_case(G, torch, kind, dtype, n0, n1, batch, rank)
     launches_per_exec = plan.launches()
     stream = torch.cuda.current_stream()
     sp = stream.cuda_stream
 
     def step():
-        plan.exec_ptr(y.data_ptr(), x.data_ptr(), False, sp)
-        plan.exec_ptr(z.data_ptr(), y.data_ptr(), True, sp)
+        for o, i, inv in execs:
+            plan.exec_ptr(o.data_ptr(), i.data_ptr(), inv, sp)
 
     for _ in range(max(3, args.warmup)):
         step()
@@ -316,20 +385,19 @@ def run_ours(args):
 
     # ---- device-resident timed region: exactly K steps
     K = args.steps
-    # one event pair per exec (forward, inverse): the dominant kernels' time
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(2 * K)]
+    E = len(execs)
+    # one event pair per exec: the time of that exec's kernels
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(E * K)]
     barrier(world)
     torch.cuda.synchronize()
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(dev) as clk:
         start.record(stream)
         for i in range(K):
-            ev[2 * i][0].record(stream)
-            plan.exec_ptr(y.data_ptr(), x.data_ptr(), False, sp)
-            ev[2 * i][1].record(stream)
-            ev[2 * i + 1][0].record(stream)
-            plan.exec_ptr(z.data_ptr(), y.data_ptr(), True, sp)
-            ev[2 * i + 1][1].record(stream)
+            for e, (o, inp, inv) in enumerate(execs):
+                ev[E * i + e][0].record(stream)
+                plan.exec_ptr(o.data_ptr(), inp.data_ptr(), inv, sp)
+                ev[E * i + e][1].record(stream)
         stop.record(stream)
         torch.cuda.synchronize()
     barrier(world)
@@ -338,40 +406,48 @@ def run_ours(args):
     launch_ms = [a.elapsed_time(b) for a, b in ev]
 
     per_transform = algo_bytes_per_transform(kind, dtype, n0, n1)
-    step_bytes = 2 * batch * per_transform
+    step_bytes = E * batch * per_transform
     gbs = world * K * step_bytes / (ms / 1e3) / 1e9
-    gflops = world * K * 2 * batch * flops_per_transform(kind, n0, n1) / (ms / 1e3) / 1e9
-    # achieved = algorithmic bytes of one exec / its device time; for plans
-    # of several launches (four-step) the exec's launches together move the
-    # exec's algorithmic bytes once
+    gflops = world * K * E * batch * flops_per_transform(kind, n0, n1) / (ms / 1e3) / 1e9
+    # achieved = algorithmic bytes of one exec / its device time; plans of
+    # several launches (four-step, 2D) move the exec's bytes once overall
     avg_exec_ms = statistics.mean(launch_ms)
     avg_launch_ms = avg_exec_ms / launches_per_exec
     peak, peak_src = measured_peak()
     achieved = batch * per_transform / (avg_exec_ms / 1e3) / 1e9
     traffic = traffic_from_profile(args.workload)
 
-    # ---- e2e through the C ABI with pinned host buffers
-    hx = torch.empty(batch, n0, dtype=cdt).pin_memory()
-    hy = torch.empty_like(hx).pin_memory()
-    hz = torch.empty_like(hx).pin_memory()
-    hx.copy_(x.cpu())
-    for _ in range(2):
-        plan.exec_host_ptr(hy.data_ptr(), hx.data_ptr(), False)
+    # ---- e2e through the C ABI (gfft_exec_host) with pinned host buffers
+    hx = x.cpu().pin_memory()
+    hy = torch.empty(y.shape, dtype=y.dtype).pin_memory()
+    hz = torch.empty(x.shape, dtype=x.dtype).pin_memory() if z is not None else None
+    hexecs = [(hy, hx, False)] + ([(hz, hy, True)] if z is not None else [])
+    for o, i, inv in hexecs:
+        plan.exec_host_ptr(o.data_ptr(), i.data_ptr(), inv)
     e2e_steps = max(1, min(K, 5))
     barrier(world)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        plan.exec_host_ptr(hy.data_ptr(), hx.data_ptr(), False)
-        plan.exec_host_ptr(hz.data_ptr(), hy.data_ptr(), True)
+        for o, i, inv in hexecs:
+            plan.exec_host_ptr(o.data_ptr(), i.data_ptr(), inv)
     t1 = time.perf_counter()
     e2e_s = max_over_ranks(world, t1 - t0)
     e2e_gbs = world * e2e_steps * step_bytes / e2e_s / 1e9
+    h2d = sum(i.numel() * i.element_size() for _, i, _ in hexecs)
+    d2h = sum(o.numel() * o.element_size() for o, _, _ in hexecs)
 
-    # sanity: the round trip reproduces n * x on a few rows
-    zz = z[:4].cpu().numpy() / n0
-    xx = x[:4].cpu().numpy()
-    rt_err = float(np.max(np.abs(zz - xx)))
-    hz_err = float(np.max(np.abs(hz[:4].numpy() / n0 - xx)))
+    # sanity on a few rows: round trip (complex) or the FP64 reference (real)
+    if z is not None:
+        npts = n0 * (n1 or 1)
+        check = float(np.max(np.abs(z.reshape(batch, -1)[:2].cpu().numpy() / npts
+                                    - x.reshape(batch, -1)[:2].cpu().numpy())))
+        e2e_check = float(np.max(np.abs(hz.reshape(batch, -1)[:2].numpy() / npts
+                                        - x.reshape(batch, -1)[:2].cpu().numpy())))
+    else:
+        xs = x[:1].cpu().numpy().astype(np.float64)
+        ref = np.fft.rfft2(xs) if kind == "r2d" else np.fft.rfft(xs)
+        check = float(np.linalg.norm(y[:1].cpu().numpy() - ref) / np.linalg.norm(ref))
+        e2e_check = float(np.linalg.norm(hy[:1].numpy() - ref) / np.linalg.norm(ref))
 
     if rank == 0:
         line = {
@@ -380,9 +456,11 @@ def run_ours(args):
             "warmup": max(3, args.warmup), "ms_per_step": round(ms / K, 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": dtype,
             "data": "synthetic",
-            "config": {"workload": args.workload, "n": n0, "batch": batch, "step": "forward+inverse",
+            "config": {"workload": args.workload, "n": n0, "height": n1 or None, "batch": batch,
+                       "step": "forward+inverse" if E == 2 else "forward",
                        "layout": "interleaved complex, contiguous batches",
-                       "l2": "inputs 512 MB per transform set > 129 MB L2; no flush",
+                       "l2": f"{x.numel() * x.element_size() >> 20} MB input per exec > 129 MB L2; no flush"
+                             if x.numel() * x.element_size() > (129 << 20) else "input fits L2",
                        "parallelism": f"replicas x{world}"},
             "gflops": round(gflops, 1),
             "hbm_frac": round(gbs / world / peak, 4),
@@ -390,15 +468,15 @@ def run_ours(args):
                          "frac": round(achieved / peak, 4), "traffic": traffic,
                          "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)" if peak_src == "measured"
                          else "fallback 6800 GB/s",
-                         "kernel": "k_c2c_fused" if launches_per_exec == 1 else "k_colpass + k_rowpass",
+                         "kernel": "k_c2c_fused" if (kind == "c2c" and launches_per_exec == 1) else "plan kernels",
                          "launches_per_exec": launches_per_exec, "avg_exec_ms": round(avg_exec_ms, 5),
                          "avg_launch_ms": round(avg_launch_ms, 5),
                          "algorithmic_bytes_per_exec": batch * per_transform},
-            "e2e": {"value": round(e2e_gbs, 2), "unit": "GB/s", "h2d_bytes_per_step": step_bytes,
-                    "d2h_bytes_per_step": step_bytes, "api": "gfft_exec_host (pinned host buffers)",
+            "e2e": {"value": round(e2e_gbs, 2), "unit": "GB/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "api": "gfft_exec_host (pinned host buffers)",
                     "steps": e2e_steps},
-            "gpu_launches": 2 * K * launches_per_exec,
-            "roundtrip_max_abs_err": rt_err, "e2e_roundtrip_max_abs_err": hz_err,
+            "gpu_launches": E * K * launches_per_exec,
+            "check": check, "e2e_check": e2e_check,
             "clocks": clk.summary(),
         }
         if not args.no_cpu:
