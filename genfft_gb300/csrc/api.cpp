@@ -30,6 +30,8 @@ thread_local std::string g_last_error;
 
 void fail(gfft_status st, const std::string &msg) { throw Error{st, msg}; }
 
+void set_last_error(const char *msg) { g_last_error = msg; }
+
 void check_cuda(cudaError_t e, const char *what)
 {
     if (e != cudaSuccess) {

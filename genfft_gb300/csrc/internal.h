@@ -18,6 +18,7 @@ struct Error {
     std::string msg;
 };
 [[noreturn]] void fail(gfft_status st, const std::string &msg);
+void set_last_error(const char *msg);  // the thread's gfft_last_error() text
 void check_cuda(cudaError_t e, const char *what);
 
 // ---- fused single-kernel C2C (c2c_fused.cu) ------------------------------
