@@ -68,6 +68,7 @@ SIGNATURES = {
     "gfft_real_fft2d_forward": [_I, _I, _I, _P, _LL, _P, _LL, _P],
     "gfft_real_fft2d_forward_2x": [_I, _I, _I, _P, _LL, _P, _LL, _P, _LL, _P],
     "gfft_separate_2x_real_fft": [_I, _I, _P, _P, _P, _P],
+    "gfft_fft_transform_noalloc": [_I, _I, _LL, _I, _P, _P, _P],
     "gfft_status_string": [_I],
     "gfft_last_error": [],
     "gfft_version": [],

@@ -155,6 +155,21 @@ gfft_status gfft_real_fft2d_forward_2x(int dtype, int width, int height, void *o
 gfft_status gfft_separate_2x_real_fft(int dtype, int n, void *out1, void *out2, const void *in,
                                       void *stream);
 
+/* Allocation-free fp32 C2C for n = 2^15 .. 2^22 (the multi-pass sizes).
+ * No counterpart in the reference: the reference computes on the host and
+ * allocates its plans' tables itself.  This variant is for callers that
+ * cannot allocate device memory when they transform (memory owned by a
+ * caching allocator or a fixed pool, or a loop where cudaMalloc would
+ * stall the device).  Its scratch and twiddle tables are fixed __device__
+ * arrays (32 MiB + ~0.3 MiB) that every GPU loading the library keeps until
+ * exit.  The first call on each device sets them up (cudaGetSymbolAddress,
+ * a synchronous table upload): make it before any stream capture.  All calls
+ * share the scratch, so calls that can overlap on the GPU race and must be
+ * serialised by the caller.  Sizes outside 2^15 .. 2^22 and fp64 are
+ * rejected.  Same results as gfft_fft_transform. */
+gfft_status gfft_fft_transform_noalloc(int dtype, int n, long long batch, int inverse, void *out,
+                                       const void *in, void *stream);
+
 const char *gfft_status_string(gfft_status status);
 /* message of the last failed call on this thread ("" if none) */
 const char *gfft_last_error(void);
