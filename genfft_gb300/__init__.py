@@ -69,6 +69,7 @@ SIGNATURES = {
     "gfft_real_fft2d_forward_2x": [_I, _I, _I, _P, _LL, _P, _LL, _P, _LL, _P],
     "gfft_separate_2x_real_fft": [_I, _I, _P, _P, _P, _P],
     "gfft_fft_transform_noalloc": [_I, _I, _LL, _I, _P, _P, _P],
+    "gfft_device_error": [ctypes.POINTER(_I)],
     "gfft_status_string": [_I],
     "gfft_last_error": [],
     "gfft_version": [],
@@ -159,6 +160,15 @@ class Plan:
             self.close()
         except Exception:
             pass
+
+
+def device_error() -> int:
+    """Read and reset the device error word (0 = no device-side timeout)."""
+    code = _I()
+    st = lib().gfft_device_error(ctypes.byref(code))
+    if st not in (0, 7):
+        _check(st)
+    return code.value
 
 
 def _check_cuda_tensor(x, name="x"):

@@ -649,6 +649,18 @@ gfft_status gfft_separate_2x_real_fft(int dtype, int n, void *out1, void *out2, 
     });
 }
 
+gfft_status gfft_device_error(int *code)
+{
+    GFFT_GUARD({
+        if (!code) fail(GFFT_ERR_INVALID_VALUE, "NULL argument");
+        unsigned v = 0, *w = device_error_word();
+        check_cuda(cudaMemcpy(&v, w, sizeof v, cudaMemcpyDeviceToHost), "read error word");
+        check_cuda(cudaMemset(w, 0, sizeof v), "reset error word");
+        *code = (int)v;
+        if (v) fail(GFFT_ERR_TIMEOUT, "a device-side wait gave up (bounded TMA wait)");
+    });
+}
+
 const char *gfft_status_string(gfft_status s)
 {
     switch (s) {

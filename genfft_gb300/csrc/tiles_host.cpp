@@ -1,7 +1,9 @@
 // tiles_host.cpp -- registry and launchers of the tile kernels.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <map>
 #include <mutex>
 #include <set>
@@ -38,7 +40,67 @@ cudaError_t ensure_smem(const void *fn, size_t smem)
     if (e == cudaSuccess) done.insert({dev, fn});
     return e;
 }
+int sm_count()
+{
+    static std::mutex mu;
+    static std::map<int, int> cache;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find(dev);
+    if (it != cache.end()) return it->second;
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 148;
+    cache[dev] = n;
+    return n;
+}
+
+bool tma_disabled()
+{
+    static const bool off = [] {
+        const char *v = std::getenv("GFFT_NO_TMA");
+        return v && *v && *v != '0';
+    }();
+    return off;
+}
+
+using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                 const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiled encode_fn()
+{
+    static EncodeTiled fn = [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return reinterpret_cast<EncodeTiled>(p);
+    }();
+    return fn;
+}
+
+bool aligned16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
+
 }  // namespace
+
+unsigned *device_error_word()
+{
+    static std::mutex mu;
+    static std::map<int, unsigned *> words;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = words.find(dev);
+    if (it != words.end()) return it->second;
+    unsigned *w = nullptr;
+    check_cuda(cudaMalloc(&w, sizeof(unsigned)), "cudaMalloc(error word)");
+    check_cuda(cudaMemset(w, 0, sizeof(unsigned)), "cudaMemset(error word)");
+    words[dev] = w;
+    return w;
+}
 
 void tile_register(int dtype, int variant, int logl, int c, const TileKernel &k)
 {
@@ -70,6 +132,35 @@ cudaError_t launch_colpass(const TileKernel &k, int inverse, long long tiles, lo
                            long long idist, long long odist, const void *tw, const void *tw_lo,
                            const void *tw_hi, int lo_bits, unsigned nmask, cudaStream_t st)
 {
+    // persistent TMA path: the tensor map needs 16-byte aligned base and
+    // strides; in-place runs (out == in) are fine, each tile is loaded whole
+    // before it is written back
+    const size_t eb = (size_t)k.elem_bytes;
+    if (k.tma_fwd && !tma_disabled() && encode_fn() && aligned16(in) && (ld_in * eb) % 16 == 0 &&
+        (nbatch == 1 || (idist * eb) % 16 == 0) && ncols * (eb / 8) < (1LL << 32) && nbatch < (1LL << 31)) {
+        const int units = (int)(eb / 8);
+        CUtensorMap map;
+        const long long rows = k.tma_rows;
+        cuuint64_t gdim[3] = {(cuuint64_t)(ncols * units), (cuuint64_t)rows, (cuuint64_t)nbatch};
+        cuuint64_t gstride[2] = {(cuuint64_t)(ld_in * eb), (cuuint64_t)((nbatch > 1 ? idist : rows * ld_in) * eb)};
+        cuuint32_t box[3] = {(cuuint32_t)(k.tma_c * units), (cuuint32_t)k.tma_boxr, 1};
+        cuuint32_t estr[3] = {1, 1, 1};
+        CUresult r = encode_fn()(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, const_cast<void *>(in), gdim, gstride,
+                                 box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                 CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r == CUDA_SUCCESS) {
+            const void *fn = inverse ? k.tma_inv : k.tma_fwd;
+            cudaError_t e = ensure_smem(fn, k.tma_smem);
+            if (e != cudaSuccess) return e;
+            unsigned *err = device_error_word();
+            long long total = tiles * nbatch;
+            long long grid = std::min<long long>(total, sm_count());
+            void *args[] = {(void *)&map, (void *)&out, (void *)&ncols, (void *)&ld_out, (void *)&odist,
+                            (void *)&nbatch, (void *)&tw, (void *)&tw_lo, (void *)&tw_hi, (void *)&lo_bits,
+                            (void *)&nmask, (void *)&err};
+            return cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(k.tma_threads), args, k.tma_smem, st);
+        }
+    }
     const void *fn = inverse ? k.inv : k.fwd;
     cudaError_t e = ensure_smem(fn, k.smem);
     if (e != cudaSuccess) return e;
@@ -92,6 +183,19 @@ cudaError_t launch_rowpass(const TileKernel &k, int inverse, long long tiles, lo
                            const void *in, void *out, long long nrows, long long ld_in, long long ostride,
                            long long idist, long long odist, const void *tw, cudaStream_t st)
 {
+    const size_t eb = (size_t)k.elem_bytes;
+    if (k.tma_fwd && !tma_disabled() && aligned16(in) && (ld_in * eb) % 16 == 0 &&
+        (nbatch == 1 || (idist * eb) % 16 == 0)) {
+        const void *fn = inverse ? k.tma_inv : k.tma_fwd;
+        cudaError_t e = ensure_smem(fn, k.tma_smem);
+        if (e != cudaSuccess) return e;
+        unsigned *err = device_error_word();
+        const long long total = tiles * nbatch;
+        const long long grid = std::min<long long>(total, sm_count());
+        void *args[] = {(void *)&in,    (void *)&out,   (void *)&nrows, (void *)&ld_in, (void *)&ostride,
+                        (void *)&idist, (void *)&odist, (void *)&nbatch, (void *)&tw, (void *)&err};
+        return cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(k.tma_threads), args, k.tma_smem, st);
+    }
     const void *fn = inverse ? k.inv : k.fwd;
     cudaError_t e = ensure_smem(fn, k.smem);
     if (e != cudaSuccess) return e;

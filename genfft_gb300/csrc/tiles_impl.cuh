@@ -3,6 +3,7 @@
 #pragma once
 
 #include "tiles.cuh"
+#include "tiles_tma.cuh"
 #include "tiles_registry.h"
 #include "twiddle.h"
 #include "../../include/genfft_gb300.h"
@@ -28,6 +29,13 @@ struct TileReg {
             k.inv = (const void *)&k_rowpass<T, LOGL, C, E, true>;
             k.threads = Cfg::THREADS;
             k.smem = Cfg::SMEM;
+            using TCfg = RowTmaCfg<T, LOGL, C, E>;
+            if constexpr (TCfg::SMEM <= 220 * 1024 && SP::N * sizeof(cpx<T>) % 16 == 0) {
+                k.tma_fwd = (const void *)&k_rowpass_tma<T, LOGL, C, E, false>;
+                k.tma_inv = (const void *)&k_rowpass_tma<T, LOGL, C, E, true>;
+                k.tma_threads = TCfg::THREADS;
+                k.tma_smem = TCfg::SMEM;
+            }
         } else {
             using Cfg = ColCfg<T, LOGL, C, E>;
             constexpr bool tw4 = V == TILE_COL_TW4, br = V == TILE_COL_BITREV, herm = V == TILE_COL_HERM;
@@ -35,6 +43,16 @@ struct TileReg {
             k.inv = (const void *)&k_colpass<T, LOGL, C, E, true, tw4, br, herm>;
             k.threads = Cfg::THREADS;
             k.smem = Cfg::SMEM;
+            using TCfg = ColTmaCfg<T, LOGL, C, E>;
+            if constexpr (!br && TCfg::SMEM <= 220 * 1024 && C * sizeof(cpx<T>) % 16 == 0) {
+                k.tma_fwd = (const void *)&k_colpass_tma<T, LOGL, C, E, false, tw4, herm>;
+                k.tma_inv = (const void *)&k_colpass_tma<T, LOGL, C, E, true, tw4, herm>;
+                k.tma_threads = TCfg::THREADS;
+                k.tma_smem = TCfg::SMEM;
+                k.tma_boxr = TCfg::BOXR;
+                k.tma_rows = TCfg::N;
+                k.tma_c = C;
+            }
         }
         k.twcount = (size_t)SP::TW;
         k.fill = &tile_fill_tw<T, LOGL, E>;

@@ -24,6 +24,14 @@ struct TileKernel {
     size_t twcount = 0;
     void (*fill)(void *) = nullptr;  // Stockham twiddles for the L-point sub-FFT
     int elem_bytes = 8;              // sizeof one complex element
+    // persistent TMA-pipelined version (nullptr when not instantiated or
+    // when its two stage buffers do not fit shared memory)
+    const void *tma_fwd = nullptr, *tma_inv = nullptr;
+    int tma_threads = 0;
+    size_t tma_smem = 0;
+    int tma_boxr = 0;  // column pass: rows per tensor box
+    int tma_rows = 0;  // column pass: column length (tensor rows)
+    int tma_c = 0;     // columns per tile
 };
 
 // register / look up (returns nullptr when not instantiated)
@@ -41,5 +49,8 @@ cudaError_t launch_colpass(const TileKernel &k, int inverse, long long tiles, lo
 cudaError_t launch_rowpass(const TileKernel &k, int inverse, long long tiles, long long nbatch,
                            const void *in, void *out, long long nrows, long long ld_in, long long ostride,
                            long long idist, long long odist, const void *tw, cudaStream_t st);
+
+// the device error word the persistent kernels report timeouts into
+unsigned *device_error_word();
 
 }  // namespace gfft

@@ -170,6 +170,12 @@ gfft_status gfft_separate_2x_real_fft(int dtype, int n, void *out1, void *out2, 
 gfft_status gfft_fft_transform_noalloc(int dtype, int n, long long batch, int inverse, void *out,
                                        const void *in, void *stream);
 
+/* Device-side error status of this device's kernels since the last call
+ * (synchronous): *code = 0 and GFFT_OK if none; otherwise the recorded
+ * code (1 = a bounded TMA wait gave up) and GFFT_ERR_TIMEOUT.  Reading
+ * resets it. */
+gfft_status gfft_device_error(int *code);
+
 const char *gfft_status_string(gfft_status status);
 /* message of the last failed call on this thread ("" if none) */
 const char *gfft_last_error(void);
