@@ -653,7 +653,8 @@ gfft_status gfft_device_error(int *code)
 {
     GFFT_GUARD({
         if (!code) fail(GFFT_ERR_INVALID_VALUE, "NULL argument");
-        unsigned v = 0, *w = device_error_word();
+        unsigned v = 0;
+        unsigned *w = device_error_word();
         check_cuda(cudaMemcpy(&v, w, sizeof v, cudaMemcpyDeviceToHost), "read error word");
         check_cuda(cudaMemset(w, 0, sizeof v), "reset error word");
         *code = (int)v;
