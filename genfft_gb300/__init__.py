@@ -54,6 +54,7 @@ SIGNATURES = {
     "gfft_plan_destroy": [_P],
     "gfft_exec": [_P, _I, _P, _P, _P],
     "gfft_exec_host": [_P, _I, _P, _P],
+    "gfft_exec_adjoint": [_P, _I, _P, _P, _P],
     "gfft_plan_launches": [_P, ctypes.POINTER(_I)],
     "gfft_plan_workspace_size": [_P, ctypes.POINTER(ctypes.c_size_t)],
     "gfft_fft_transform": [_I, _I, _LL, _I, _P, _P, _P],
@@ -140,6 +141,13 @@ class Plan:
     def exec(self, out, x, inverse: bool = False, stream=None):
         """Run on torch CUDA tensors (current stream)."""
         self.exec_ptr(out.data_ptr(), x.data_ptr(), inverse, _stream_ptr(stream))
+        return out
+
+    def adjoint_ptr(self, out_ptr: int, in_ptr: int, inverse: bool = False, stream_ptr: int = 0):
+        _check(lib().gfft_exec_adjoint(self._h, int(inverse), out_ptr, in_ptr, stream_ptr))
+
+    def adjoint(self, out, g, inverse: bool = False, stream=None):
+        self.adjoint_ptr(out.data_ptr(), g.data_ptr(), inverse, _stream_ptr(stream))
         return out
 
     def exec_host_ptr(self, out_ptr: int, in_ptr: int, inverse: bool = False):

@@ -190,6 +190,7 @@ static gfft_plan_s *make_plan(const gfft_desc &in)
             break;
         case GFFT_KIND_R2C:
             p->r2c.init(d.dtype, ilog2ll(d.n0), half ? 1 : 0, d.batch);
+            p->c2r.init(d.dtype, ilog2ll(d.n0), d.batch);
             p->launches = p->r2c.launches(d.batch);
             break;
         case GFFT_KIND_C2C_2D:
@@ -210,6 +211,7 @@ static gfft_plan_s *make_plan(const gfft_desc &in)
     } catch (...) {
         p->c2c.release();
         p->r2c.release();
+        p->c2r.release();
         throw;
     }
     return p.release();
@@ -241,9 +243,10 @@ static void exec_plan(gfft_plan_s &p, int inverse, void *out, const void *in, co
 {
     const gfft_desc &d = p.d;
     const size_t cb = cplx_bytes(d.dtype), rb = real_bytes(d.dtype);
-    const bool real_in = d.kind == GFFT_KIND_R2C || d.kind == GFFT_KIND_R2C_2D;
+    const bool real_in = (d.kind == GFFT_KIND_R2C && !inverse) || d.kind == GFFT_KIND_R2C_2D;
+    const bool real_out = d.kind == GFFT_KIND_R2C && inverse;
     check_ptr(in, real_in ? rb : cb, "in");
-    check_ptr(out, cb, "out");
+    check_ptr(out, real_out ? rb : cb, "out");
     switch (d.kind) {
     case GFFT_KIND_C2C:
         if (d.flags & GFFT_FLAG_BITREV_INPUT) {
@@ -261,7 +264,14 @@ static void exec_plan(gfft_plan_s &p, int inverse, void *out, const void *in, co
         }
         break;
     case GFFT_KIND_R2C: {
-        if (inverse) fail(GFFT_ERR_UNSUPPORTED, "the real-input transform has no inverse (FFTReal.h:186-221)");
+        if (inverse) {
+            // half-spectrum inverse: the plan's output layout is the input
+            // (bins), its input layout the output (reals); unscaled
+            if (overlaps(in, (size_t)(L.batch * L.odist) * cb, out, (size_t)(L.batch * L.idist) * rb))
+                fail(GFFT_ERR_ALIAS, "half-spectrum inverse: output must not overlap the input");
+            p.c2r.run(in, out, L.batch, L.odist, L.idist, 0, st);
+            break;
+        }
         if (overlaps(in, (size_t)(L.batch * L.idist) * rb, out, (size_t)(L.batch * L.odist) * cb))
             fail(GFFT_ERR_ALIAS, "real-input transform: output must not overlap the input");
         p.r2c.run(in, out, L.batch, L.idist, L.odist, st);
@@ -307,6 +317,46 @@ static void exec_plan(gfft_plan_s &p, int inverse, void *out, const void *in, co
     }
     default:
         fail(GFFT_ERR_INVALID_PLAN, "plan has no transform kind");
+    }
+}
+
+// Adjoint of the plan's transform in direction `inverse` (reverse-mode
+// differentiation: grad_in = A^H grad_out in PyTorch's convention).
+static void exec_adjoint(gfft_plan_s &p, int inverse, void *out, const void *in, const Layout &L, cudaStream_t st)
+{
+    const gfft_desc &d = p.d;
+    switch (d.kind) {
+    case GFFT_KIND_C2C:
+    case GFFT_KIND_C2C_2D:
+    case GFFT_KIND_VERT: {
+        // the unnormalised DFT's adjoint is the conjugate-direction (unscaled
+        // inverse) transform; the output layout becomes the input layout
+        if (d.flags & GFFT_FLAG_BITREV_INPUT) fail(GFFT_ERR_UNSUPPORTED, "adjoint of a bit-reversed-input plan");
+        Layout A{L.batch, L.ostride, L.odist, L.istride, L.idist};
+        exec_plan(p, !inverse, out, in, A, st);
+        break;
+    }
+    case GFFT_KIND_R2C: {
+        const size_t cb = cplx_bytes(d.dtype), rb = real_bytes(d.dtype);
+        if (!inverse) {
+            // adjoint of R2C: C2R of the gradient with interior bins halved
+            // (half spectrum) or folded (full spectrum)
+            check_ptr(in, cb, "in");
+            check_ptr(out, rb, "out");
+            const int w = (d.flags & GFFT_FLAG_HALF_SPECTRUM) ? 1 : 2;
+            p.c2r.run(in, out, L.batch, L.odist, L.idist, w, st);
+        } else {
+            // adjoint of the half-spectrum C2R: R2C with interior bins doubled
+            check_ptr(in, rb, "in");
+            check_ptr(out, cb, "out");
+            if (!(d.flags & GFFT_FLAG_HALF_SPECTRUM))
+                fail(GFFT_ERR_UNSUPPORTED, "adjoint of the inverse needs a half-spectrum plan");
+            p.r2c.run(in, out, L.batch, L.idist, L.odist, st, 2);
+        }
+        break;
+    }
+    default:
+        fail(GFFT_ERR_UNSUPPORTED, "no adjoint for this transform kind");
     }
 }
 
@@ -369,6 +419,7 @@ static void destroy_plan(gfft_plan_s *p)
     }
     p->c2c.release();
     p->r2c.release();
+    p->c2r.release();
     p->magic = 0;
     delete p;
 }
@@ -457,6 +508,14 @@ gfft_status gfft_exec(gfft_plan plan, int inverse, void *out, const void *in, vo
     GFFT_GUARD({
         gfft_plan_s *p = checked(plan);
         exec_plan(*p, inverse != 0, out, in, plan_layout(*p), (cudaStream_t)stream);
+    });
+}
+
+gfft_status gfft_exec_adjoint(gfft_plan plan, int inverse, void *out, const void *in, void *stream)
+{
+    GFFT_GUARD({
+        gfft_plan_s *p = checked(plan);
+        exec_adjoint(*p, inverse != 0, out, in, plan_layout(*p), (cudaStream_t)stream);
     });
 }
 

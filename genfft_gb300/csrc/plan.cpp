@@ -174,20 +174,70 @@ int R2CCore::launches(long long batch) const
     return 1;
 }
 
-void R2CCore::run(const void *in, void *out, long long batch, long long idist, long long odist,
-                  cudaStream_t st) const
+void R2CCore::run(const void *in, void *out, long long batch, long long idist, long long odist, cudaStream_t st,
+                  int mode) const
 {
+    if (mode < 0) mode = half ? 0 : 1;
     if (algo == 0) {
         check_cuda(launch_r2c_one(dtype, in, out, batch, idist, odist, st), "launch R2C n=1");
     } else if (algo == 1) {
-        check_cuda(launch_r2c_fused(dtype, logn - 1, half, in, out, batch, idist, odist, tw, dtw, st),
+        check_cuda(launch_r2c_fused(dtype, logn - 1, mode, in, out, batch, idist, odist, tw, dtw, st),
                    "launch fused R2C");
     } else {
         const long long H = 1LL << (logn - 1);
         // n reals are n/2 complex; transform them into the output buffer,
         // then adjust in place (the reference's order, FFTReal.h:209-211)
         c2c.run(0, in, out, batch, idist / 2, odist, 1, 1, st);
-        check_cuda(launch_dit(dtype, half, out, out, H, batch, odist, odist, dtw, st), "launch DIT pass");
+        check_cuda(launch_dit(dtype, mode, out, out, H, batch, odist, odist, dtw, st), "launch DIT pass");
+    }
+}
+
+// ---------------------------------------------------------------------------
+// half-spectrum inverse
+
+void C2RCore::init(int dtype_, int logn_, long long batch_hint)
+{
+    dtype = dtype_;
+    logn = logn_;
+    if (logn == 0) {
+        algo = 0;
+        return;
+    }
+    const int d = dtype, l = logn, lh = logn - 1;
+    dtw = cached_table("dit/" + std::to_string(d) + "/" + std::to_string(l), d, (1LL << lh) + 1,
+                       [d, l](void *buf) { dit_twiddle_fill(d, l, buf); });
+    if (lh <= c2r_fused_max_logh(dtype)) {
+        // the fused C2R runs the same Stockham plan (points per thread) as
+        // the fused R2C of this half length, so it shares that table
+        algo = 1;
+        tw = cached_table("r2c/" + std::to_string(d) + "/" + std::to_string(lh), d, r2c_twiddle_count(d, lh),
+                          [d, lh](void *buf) { r2c_twiddle_fill(d, lh, buf); });
+        return;
+    }
+    algo = 2;
+    c2c.init(dtype, lh, batch_hint);
+}
+
+int C2RCore::launches(long long batch) const
+{
+    if (algo == 2) return c2c.launches(batch) + 1;
+    return 1;
+}
+
+void C2RCore::run(const void *in, void *out, long long batch, long long idist, long long odist, int wmode,
+                  cudaStream_t st) const
+{
+    if (algo == 0) {
+        check_cuda(launch_c2r_one(dtype, in, out, batch, idist, odist, st), "launch C2R n=1");
+    } else if (algo == 1) {
+        check_cuda(launch_c2r_fused(dtype, logn - 1, wmode, in, out, batch, idist, odist, tw, dtw, st),
+                   "launch fused C2R");
+    } else {
+        const long long H = 1LL << (logn - 1);
+        // Z' (n/2 complex = the n output reals) into the output buffer, then
+        // the unscaled inverse C2C of n/2 points in place
+        check_cuda(launch_c2r_pre(dtype, wmode, in, out, H, batch, idist, odist / 2, dtw, st), "launch C2R pre-pass");
+        c2c.run(1, out, out, batch, odist / 2, odist / 2, 1, 1, st);
     }
 }
 

@@ -47,6 +47,7 @@ struct ColCore {
 };
 
 // Real-input 1D transform of n = 2^logn reals (RealFFT<T>::forward).
+// mode: 0 half spectrum, 1 full spectrum, 2 half with doubled interior bins
 struct R2CCore {
     int dtype = 0, logn = 0, half = 1;
     int algo = 0;  // 0 n == 1, 1 fused, 2 C2C(n/2) + DIT pass
@@ -56,7 +57,23 @@ struct R2CCore {
     void release() { c2c.release(); }
     int launches(long long batch) const;
     // idist in reals (even), odist in complex elements
-    void run(const void *in, void *out, long long batch, long long idist, long long odist, cudaStream_t st) const;
+    void run(const void *in, void *out, long long batch, long long idist, long long odist, cudaStream_t st,
+             int mode = -1) const;
+};
+
+// Half-spectrum inverse: n/2+1 bins -> n reals, unscaled, Hermitian
+// extension (imaginary parts of the DC and Nyquist bins ignored)
+struct C2RCore {
+    int dtype = 0, logn = 0;
+    int algo = 0;  // 0 n == 1, 1 fused, 2 pre-pass + C2C(n/2) inverse
+    const void *tw = nullptr, *dtw = nullptr;
+    C2CCore c2c;
+    void init(int dtype, int logn, long long batch_hint);
+    void release() { c2c.release(); }
+    int launches(long long batch) const;
+    // idist in complex elements, odist in reals (even)
+    void run(const void *in, void *out, long long batch, long long idist, long long odist, int wmode,
+             cudaStream_t st) const;
 };
 
 // ---- kernels in real.cu --------------------------------------------------
@@ -64,10 +81,22 @@ int r2c_fused_max_logh(int dtype);
 size_t r2c_twiddle_count(int dtype, int logh);
 void r2c_twiddle_fill(int dtype, int logh, void *buf);
 void dit_twiddle_fill(int dtype, int logn, void *buf);
-cudaError_t launch_r2c_fused(int dtype, int logh, int half, const void *in, void *out, long long batch,
+// mode: 0 half spectrum, 1 full spectrum, 2 half with doubled interior
+// bins (the adjoint of the half-spectrum C2R)
+cudaError_t launch_r2c_fused(int dtype, int logh, int mode, const void *in, void *out, long long batch,
                              long long idist, long long odist, const void *tw, const void *dtw, cudaStream_t st);
-cudaError_t launch_dit(int dtype, int half, const void *in, void *out, long long H, long long batch,
+cudaError_t launch_dit(int dtype, int mode, const void *in, void *out, long long H, long long batch,
                        long long idist, long long odist, const void *dtw, cudaStream_t st);
+// C2R (c2r.cu): weighting 0 = as given (Hermitian extension), 1 = interior
+// bins halved (adjoint of the half-spectrum R2C), 2 = n-bin input folded
+// (g_k + conj g_{n-k}) / 2 (adjoint of the full-spectrum R2C)
+int c2r_fused_max_logh(int dtype);
+cudaError_t launch_c2r_fused(int dtype, int logh, int wmode, const void *in, void *out, long long batch,
+                             long long idist, long long odist, const void *tw, const void *dtw, cudaStream_t st);
+cudaError_t launch_c2r_pre(int dtype, int wmode, const void *in, void *out, long long H, long long batch,
+                           long long idist, long long odist, const void *dtw, cudaStream_t st);
+cudaError_t launch_c2r_one(int dtype, const void *in, void *out, long long batch, long long idist, long long odist,
+                           cudaStream_t st);
 cudaError_t launch_dit_one(int dtype, const void *in, void *out, cudaStream_t st);
 cudaError_t launch_r2c_one(int dtype, const void *in, void *out, long long batch, long long idist, long long odist,
                            cudaStream_t st);
@@ -87,6 +116,7 @@ struct gfft_plan_s {
     gfft::C2CCore c2c;   // C2C; 2D row pass
     gfft::ColCore col;   // 2D column pass; VERT
     gfft::R2CCore r2c;   // R2C; real-2D row pass
+    gfft::C2RCore c2r;   // C2R; adjoint of R2C
     // host-path staging (owned, lazily allocated)
     std::mutex host_mu;
     void *stage[3] = {nullptr, nullptr, nullptr};

@@ -53,8 +53,22 @@ __device__ __forceinline__ cpx<T> dit_value(cpx<T> zk, cpx<T> zj, cpx<T> t)
     return {e.x - to.x, e.y - to.y};
 }
 
+// output modes of the real-input kernels
+enum R2CMode { R2C_HALF = 0, R2C_FULL = 1, R2C_HALF_X2 = 2 };
+// R2C_HALF_X2 doubles bins 1..n/2-1 (and keeps the real DC / Nyquist bins):
+// it is the adjoint of the half-spectrum C2R (c2r.cu), whose output counts
+// each interior bin twice through the Hermitian extension.
+template <int MODE, typename T>
+__device__ __forceinline__ cpx<T> r2c_weight(cpx<T> f, long long k, long long H)
+{
+    if constexpr (MODE == R2C_HALF_X2) {
+        if (k > 0 && k < H) return {f.x + f.x, f.y + f.y};
+    }
+    return f;
+}
+
 // in: reals (idist reals between transforms, even), out: complex (odist)
-template <typename T, int LOGH, bool HALF>
+template <typename T, int LOGH, int MODE>
 __global__ void __launch_bounds__(R2CCfg<T, LOGH>::THREADS)
     k_r2c_fused(const T *__restrict__ in, cpx<T> *__restrict__ out, long long batch, long long idist,
                 long long odist, const cpx<T> *__restrict__ tw, const cpx<T> *__restrict__ dtw)
@@ -94,8 +108,8 @@ __global__ void __launch_bounds__(R2CCfg<T, LOGH>::THREADS)
         const int km = k & (H - 1);
         const int j = (H - k) & (H - 1);
         const cpx<T> f = dit_value(my[spad<T>(km)], my[spad<T>(j)], ldg_c(dtw + k));
-        stcs_c(dst + k, f);
-        if constexpr (!HALF) {
+        stcs_c(dst + k, r2c_weight<MODE>(f, k, H));
+        if constexpr (MODE == R2C_FULL) {
             if (k > 0 && k < H) stcs_c(dst + 2 * H - k, conj(f));
         }
     }
@@ -104,7 +118,7 @@ __global__ void __launch_bounds__(R2CCfg<T, LOGH>::THREADS)
 // Stand-alone adjustment (DIT<T>::apply, fft.h:180-188), in place or not:
 // thread p handles the pair (k, H - k), k = p in [0, H/2], reading both Z
 // values before writing, so out == in is safe.
-template <typename T, bool HALF>
+template <typename T, int MODE>
 __global__ void k_dit(const cpx<T> *in, cpx<T> *out, long long H, long long batch, long long idist,
                       long long odist, const cpx<T> *__restrict__ dtw)
 {
@@ -119,9 +133,9 @@ __global__ void k_dit(const cpx<T> *in, cpx<T> *out, long long H, long long batc
         const cpx<T> zk = ld_c(z + (k & (H - 1))), zj = ld_c(z + j);
         const cpx<T> fk = dit_value(zk, zj, ldg_c(dtw + k));
         const cpx<T> fj = dit_value(zj, zk, ldg_c(dtw + (H - k)));
-        st_c(f + k, fk);
-        if (H - k != k) st_c(f + (H - k), fj);
-        if constexpr (!HALF) {
+        st_c(f + k, r2c_weight<MODE>(fk, k, H));
+        if (H - k != k) st_c(f + (H - k), r2c_weight<MODE>(fj, H - k, H));
+        if constexpr (MODE == R2C_FULL) {
             if (k > 0) st_c(f + 2 * H - k, conj(fk));
             if (k > 0 && H - k != k) st_c(f + H + k, conj(fj));
         }
@@ -222,7 +236,7 @@ cudaError_t smem_optin(const void *fn, size_t smem)
 }
 
 struct R2CEntry {
-    const void *half, *full;
+    const void *fn[3];
     int threads, tpc;
     size_t smem, twcount;
     void (*fill)(void *);
@@ -239,7 +253,8 @@ template <typename T, int LOGH>
 R2CEntry make_r2c()
 {
     using Cfg = R2CCfg<T, LOGH>;
-    return R2CEntry{(const void *)&k_r2c_fused<T, LOGH, true>, (const void *)&k_r2c_fused<T, LOGH, false>,
+    return R2CEntry{{(const void *)&k_r2c_fused<T, LOGH, R2C_HALF>, (const void *)&k_r2c_fused<T, LOGH, R2C_FULL>,
+                     (const void *)&k_r2c_fused<T, LOGH, R2C_HALF_X2>},
                     Cfg::THREADS, Cfg::TPC, Cfg::SMEM, (size_t)Cfg::SP::TW, &r2c_fill<T, LOGH>};
 }
 
@@ -288,11 +303,11 @@ void dit_twiddle_fill(int dtype, int logn, void *buf)
     }
 }
 
-cudaError_t launch_r2c_fused(int dtype, int logh, int half, const void *in, void *out, long long batch,
+cudaError_t launch_r2c_fused(int dtype, int logh, int mode, const void *in, void *out, long long batch,
                              long long idist, long long odist, const void *tw, const void *dtw, cudaStream_t st)
 {
     const R2CEntry &e = r2c_entry(dtype, logh);
-    const void *fn = half ? e.half : e.full;
+    const void *fn = e.fn[mode];
     cudaError_t err = smem_optin(fn, e.smem);
     if (err != cudaSuccess) return err;
     const long long grid = (batch + e.tpc - 1) / e.tpc;
@@ -301,17 +316,24 @@ cudaError_t launch_r2c_fused(int dtype, int logh, int half, const void *in, void
     return cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(e.threads), args, e.smem, st);
 }
 
-cudaError_t launch_dit(int dtype, int half, const void *in, void *out, long long H, long long batch,
+template <typename T>
+void dit_launch(int mode, unsigned g, const void *in, void *out, long long H, long long batch, long long idist,
+                long long odist, const void *dtw, cudaStream_t st)
+{
+    auto i = (const cpx<T> *)in;
+    auto o = (cpx<T> *)out;
+    auto d = (const cpx<T> *)dtw;
+    if (mode == R2C_HALF) k_dit<T, R2C_HALF><<<g, 256, 0, st>>>(i, o, H, batch, idist, odist, d);
+    else if (mode == R2C_FULL) k_dit<T, R2C_FULL><<<g, 256, 0, st>>>(i, o, H, batch, idist, odist, d);
+    else k_dit<T, R2C_HALF_X2><<<g, 256, 0, st>>>(i, o, H, batch, idist, odist, d);
+}
+
+cudaError_t launch_dit(int dtype, int mode, const void *in, void *out, long long H, long long batch,
                        long long idist, long long odist, const void *dtw, cudaStream_t st)
 {
     const unsigned g = grid_for((H / 2 + 1) * batch, 256);
-    if (dtype == GFFT_F32) {
-        if (half) k_dit<float, true><<<g, 256, 0, st>>>((const cpx<float> *)in, (cpx<float> *)out, H, batch, idist, odist, (const cpx<float> *)dtw);
-        else k_dit<float, false><<<g, 256, 0, st>>>((const cpx<float> *)in, (cpx<float> *)out, H, batch, idist, odist, (const cpx<float> *)dtw);
-    } else {
-        if (half) k_dit<double, true><<<g, 256, 0, st>>>((const cpx<double> *)in, (cpx<double> *)out, H, batch, idist, odist, (const cpx<double> *)dtw);
-        else k_dit<double, false><<<g, 256, 0, st>>>((const cpx<double> *)in, (cpx<double> *)out, H, batch, idist, odist, (const cpx<double> *)dtw);
-    }
+    if (dtype == GFFT_F32) dit_launch<float>(mode, g, in, out, H, batch, idist, odist, dtw, st);
+    else dit_launch<double>(mode, g, in, out, H, batch, idist, odist, dtw, st);
     return cudaGetLastError();
 }
 

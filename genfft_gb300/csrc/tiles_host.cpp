@@ -84,6 +84,29 @@ EncodeTiled encode_fn()
 
 bool aligned16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
 
+// persistent grid: every CTA that fits on the GPU at once (cached per kernel)
+long long persistent_grid(const void *fn, int threads, size_t smem, long long work)
+{
+    static std::mutex mu;
+    static std::map<std::pair<int, const void *>, int> occ;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int per_sm = 1;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        auto it = occ.find({dev, fn});
+        if (it != occ.end()) {
+            per_sm = it->second;
+        } else {
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem) != cudaSuccess ||
+                per_sm < 1)
+                per_sm = 1;
+            occ[{dev, fn}] = per_sm;
+        }
+    }
+    return std::max<long long>(1, std::min<long long>(work, (long long)sm_count() * per_sm));
+}
+
 }  // namespace
 
 unsigned *device_error_word()
@@ -118,13 +141,20 @@ const TileKernel *tile_find(int dtype, int variant, int logl, int c)
 int tile_widest(int dtype, int variant, int logl, int max_c)
 {
     std::lock_guard<std::mutex> lk(reg_mu());
-    int best = 0;
+    int best = 0, best_tma = 0, narrowest = 0;
     for (auto &kv : registry()) {
-        if (std::get<0>(kv.first) == dtype && std::get<1>(kv.first) == variant &&
-            std::get<2>(kv.first) == logl && std::get<3>(kv.first) <= max_c)
-            best = std::max(best, std::get<3>(kv.first));
+        if (std::get<0>(kv.first) != dtype || std::get<1>(kv.first) != variant || std::get<2>(kv.first) != logl)
+            continue;
+        const int c = std::get<3>(kv.first);
+        if (!narrowest || c < narrowest) narrowest = c;
+        if (c > max_c) continue;
+        best = std::max(best, c);
+        if (kv.second.tma_fwd) best_tma = std::max(best_tma, c);
     }
-    return best;
+    // prefer the widest tile that has a TMA-pipelined version; else the
+    // widest under the cap; else the narrowest there is
+    if (best_tma && !tma_disabled()) return best_tma;
+    return best ? best : narrowest;
 }
 
 cudaError_t launch_colpass(const TileKernel &k, int inverse, long long tiles, long long nbatch,
@@ -153,8 +183,7 @@ cudaError_t launch_colpass(const TileKernel &k, int inverse, long long tiles, lo
             cudaError_t e = ensure_smem(fn, k.tma_smem);
             if (e != cudaSuccess) return e;
             unsigned *err = device_error_word();
-            long long total = tiles * nbatch;
-            long long grid = std::min<long long>(total, sm_count());
+            const long long grid = persistent_grid(fn, k.tma_threads, k.tma_smem, tiles * nbatch);
             void *args[] = {(void *)&map, (void *)&out, (void *)&ncols, (void *)&ld_out, (void *)&odist,
                             (void *)&nbatch, (void *)&tw, (void *)&tw_lo, (void *)&tw_hi, (void *)&lo_bits,
                             (void *)&nmask, (void *)&err};
@@ -190,8 +219,7 @@ cudaError_t launch_rowpass(const TileKernel &k, int inverse, long long tiles, lo
         cudaError_t e = ensure_smem(fn, k.tma_smem);
         if (e != cudaSuccess) return e;
         unsigned *err = device_error_word();
-        const long long total = tiles * nbatch;
-        const long long grid = std::min<long long>(total, sm_count());
+        const long long grid = persistent_grid(fn, k.tma_threads, k.tma_smem, tiles * nbatch);
         void *args[] = {(void *)&in,    (void *)&out,   (void *)&nrows, (void *)&ld_in, (void *)&ostride,
                         (void *)&idist, (void *)&odist, (void *)&nbatch, (void *)&tw, (void *)&err};
         return cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(k.tma_threads), args, k.tma_smem, st);

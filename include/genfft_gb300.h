@@ -86,8 +86,19 @@ typedef struct gfft_plan_s *gfft_plan;
  * read-only tables.  Creation is thread-safe. */
 gfft_status gfft_plan_create(gfft_plan *plan, const gfft_desc *desc);
 gfft_status gfft_plan_destroy(gfft_plan plan);
-/* forward (inverse = 0) or unscaled inverse (inverse = 1) on device memory */
+/* forward (inverse = 0) or unscaled inverse (inverse = 1) on device memory.
+ * For GFFT_KIND_R2C plans the inverse is the half-spectrum inverse (C2R):
+ * bins in the plan's output layout -> reals in its input layout, unscaled,
+ * imaginary parts of the DC and Nyquist bins ignored (no counterpart in the
+ * reference, whose RealFFT has no inverse, FFTReal.h:127-130). */
 gfft_status gfft_exec(gfft_plan plan, int inverse, void *out, const void *in, void *stream);
+/* Adjoint (reverse-mode gradient) of the plan's transform in direction
+ * `inverse`: grad_in = A^H grad_out with PyTorch's complex convention.
+ * C2C / 2D / VERT: the conjugate-direction transform.  R2C forward: a C2R of
+ * the gradient with the Hermitian weighting (interior bins halved, or the
+ * full spectrum folded); C2R: an R2C with interior bins doubled.  `in` has
+ * the layout of the transform's output, `out` that of its input. */
+gfft_status gfft_exec_adjoint(gfft_plan plan, int inverse, void *out, const void *in, void *stream);
 /* Same transform on HOST buffers (the reference's calling convention):
  * copies in, transforms and copies out in pipelined chunks, synchronously.
  * Pinned host memory gives full link bandwidth; pageable memory works. */
