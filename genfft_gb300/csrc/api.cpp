@@ -631,7 +631,7 @@ gfft_status gfft_dit_apply(int dtype, int n, void *out, const void *in, int half
             const void *dtw = cached_table("dit/" + std::to_string(dtype) + "/" + std::to_string(logn), dtype,
                                            (size_t)n / 2 + 1,
                                            [dtype, logn](void *buf) { dit_twiddle_fill(dtype, logn, buf); });
-            check_cuda(launch_dit(dtype, half != 0, in, out, n / 2, 1, n, n, dtw, (cudaStream_t)stream), "DIT");
+            check_cuda(launch_dit(dtype, half ? 0 : 1, in, out, n / 2, 1, n, n, dtw, (cudaStream_t)stream), "DIT");
         }
     });
 }

@@ -22,9 +22,16 @@ def loss_np(x, w, kind, n=None, half=True):
 
 
 def fd_check(loss, x, grad, coords, h=1e-6, complex_x=False):
+    """Largest |FD - analytic| over the coordinates, in units of the
+    allowed error: 1e-6 of the RMS gradient plus the FP64 rounding noise of
+    the central difference (the loss is summed from ~n terms, so its
+    rounding error is a few ulp of |loss|, divided by 2h)."""
     flat = x.reshape(-1).copy()
     g = grad.reshape(-1)
-    errs = []
+    l0 = abs(loss(x))
+    noise = 16 * np.finfo(np.float64).eps * l0 / (2 * h)
+    allow = 1e-6 * np.sqrt(np.mean(np.abs(g) ** 2)) + noise
+    worst = 0.0
     for c in coords:
         parts = [(1, "re")] + ([(1j, "im")] if complex_x else [])
         for unit, name in parts:
@@ -32,8 +39,8 @@ def fd_check(loss, x, grad, coords, h=1e-6, complex_x=False):
             xm = flat.copy(); xm[c] -= unit * h
             fd = (loss(xp.reshape(x.shape)) - loss(xm.reshape(x.shape))) / (2 * h)
             an = g[c].real if name == "re" else g[c].imag
-            errs.append(abs(fd - an) / (abs(fd) + 1e-3 * np.max(np.abs(g)) + 1e-30))
-    return max(errs)
+            worst = max(worst, abs(fd - an) / allow)
+    return worst
 
 
 @pytest.mark.parametrize("n,inverse", [(64, False), (1024, False), (4096, True), (1 << 16, False)])
@@ -59,7 +66,7 @@ def test_c2c_gradient(gfft, n, inverse):
     coords = rng.choice(xn.size, 64, replace=False)
     kind = "ic2c" if inverse else "c2c"
     err = fd_check(lambda v: loss_np(v, wn, kind), xn, an, coords, complex_x=True)
-    assert err < 1e-4, err
+    assert err < 1, err
 
 
 @pytest.mark.parametrize("n,half", [(2, True), (8, True), (64, False), (4096, True), (4096, False),
@@ -87,7 +94,7 @@ def test_r2c_gradient_hermitian_weighting(gfft, n, half):
     assert rel < 2e-6 * max(1, np.log2(n)), rel
     coords = rng.choice(xn.size, min(64, xn.size), replace=False)
     err = fd_check(lambda v: loss_np(v, wn, "r2c", half=half), xn, an, coords)
-    assert err < 1e-4, err
+    assert err < 1, err
 
 
 @pytest.mark.parametrize("n", [2, 16, 4096, 1 << 17])

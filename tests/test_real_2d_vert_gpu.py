@@ -246,9 +246,9 @@ def test_alias_errors(gfft):
     with pytest.raises(gfft.GFFTError) as e:
         gfft._check(gfft.lib().gfft_real_fft_forward(0, 64, 1, xr.data_ptr(), xr.data_ptr(), 1, 0))
     assert e.value.name == "GFFT_ERR_ALIAS"
-    # the real-input transform has no inverse (FFTReal.h:186-221)
-    p = gfft.Plan(gfft.KIND_R2C, gfft.F32, 64, 0, 1)
-    out = torch.zeros(64, dtype=torch.complex64, device="cuda")
+    # RealFFT2D has no inverse (FFTReal.h:127-130)
+    p = gfft.Plan(gfft.KIND_R2C_2D, gfft.F32, 64, 4, 1)
+    out = torch.zeros(4, 64, dtype=torch.complex64, device="cuda")
     with pytest.raises(gfft.GFFTError) as e:
         p.exec_ptr(out.data_ptr(), xr.data_ptr(), True, 0)
     assert e.value.name == "GFFT_ERR_UNSUPPORTED"
