@@ -71,6 +71,12 @@ SIGNATURES = {
     "gfft_separate_2x_real_fft": [_I, _I, _P, _P, _P, _P],
     "gfft_fft_transform_noalloc": [_I, _I, _LL, _I, _P, _P, _P],
     "gfft_device_error": [ctypes.POINTER(_I)],
+    "gfft_ragged_create": [ctypes.POINTER(_P), _I, ctypes.POINTER(_LL), _LL],
+    "gfft_ragged_destroy": [_P],
+    "gfft_ragged_exec": [_P, _I, _P, _P, _P],
+    "gfft_ragged_exec_adjoint": [_P, _I, _P, _P, _P],
+    "gfft_ragged_autotune": [_P, _P, _P, _P, ctypes.POINTER(_I), ctypes.POINTER(ctypes.c_double)],
+    "gfft_ragged_elements": [_P, ctypes.POINTER(_LL)],
     "gfft_status_string": [_I],
     "gfft_last_error": [],
     "gfft_version": [],
@@ -345,3 +351,50 @@ def rfft2_2x(a, b):
     _check(lib().gfft_real_fft2d_forward_2x(_dtype_code(a), W, H, out.data_ptr(), W, a.data_ptr(), W,
                                             b.data_ptr(), W, _stream_ptr()))
     return out
+
+
+class RaggedPlan:
+    """Ragged batch of fp32 C2C transforms (sizes powers of two, 1..2^18)
+    packed back to back; one persistent graph-captured launch per exec."""
+
+    def __init__(self, sizes):
+        self.sizes = [int(s) for s in sizes]
+        arr = (_LL * len(self.sizes))(*self.sizes)
+        h = _P()
+        _check(lib().gfft_ragged_create(ctypes.byref(h), F32, arr, len(self.sizes)))
+        self._h = h
+        n = _LL()
+        _check(lib().gfft_ragged_elements(self._h, ctypes.byref(n)))
+        self.elements = n.value
+        offs, pos = [], 0
+        for s in self.sizes:
+            offs.append(pos)
+            pos += s
+        self.offsets = offs
+
+    def exec(self, out, x, inverse: bool = False, stream=None):
+        _check(lib().gfft_ragged_exec(self._h, int(inverse), out.data_ptr(), x.data_ptr(), _stream_ptr(stream)))
+        return out
+
+    def adjoint(self, out, g, inverse: bool = False, stream=None):
+        _check(lib().gfft_ragged_exec_adjoint(self._h, int(inverse), out.data_ptr(), g.data_ptr(),
+                                              _stream_ptr(stream)))
+        return out
+
+    def autotune(self, out, x, stream=None):
+        params = (_I * 3)()
+        ms = ctypes.c_double()
+        _check(lib().gfft_ragged_autotune(self._h, out.data_ptr(), x.data_ptr(), _stream_ptr(stream), params,
+                                          ctypes.byref(ms)))
+        return list(params), ms.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().gfft_ragged_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -128,3 +128,28 @@ def rfft(x, half: bool = True):
 def irfft(y, n: int):
     """Differentiable unscaled half-spectrum inverse."""
     return IRFFTFunction.apply(y, n)
+
+
+class RaggedFFTFunction(torch.autograd.Function):
+    """Ragged batch (packed 1D complex64 tensor) through a RaggedPlan; the
+    backward pass is the plan's adjoint (conjugate-direction) launch."""
+
+    @staticmethod
+    def forward(ctx, x, plan, inverse: bool = False):
+        x = x.contiguous()
+        y = torch.empty_like(x)
+        plan.exec(y, x, inverse)
+        ctx.plan, ctx.inverse = plan, inverse
+        return y
+
+    @staticmethod
+    def backward(ctx, g):
+        g = g.contiguous()
+        gx = torch.empty_like(g)
+        ctx.plan.adjoint(gx, g, ctx.inverse)
+        return gx, None, None
+
+
+def ragged_fft(x, plan, inverse: bool = False):
+    """Differentiable ragged batch transform (see genfft_gb300.RaggedPlan)."""
+    return RaggedFFTFunction.apply(x, plan, inverse)

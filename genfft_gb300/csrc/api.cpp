@@ -456,9 +456,9 @@ static gfft_plan_s *cached_plan(int kind, int dtype, long long n0, long long n1,
 
 using namespace gfft;
 
-#define GFFT_GUARD(body)                         \
+#define GFFT_GUARD(...)                          \
     try {                                        \
-        body;                                    \
+        __VA_ARGS__;                             \
         return GFFT_OK;                          \
     } catch (const Error &e) {                   \
         g_last_error = e.msg;                    \
@@ -705,6 +705,62 @@ gfft_status gfft_separate_2x_real_fft(int dtype, int n, void *out1, void *out2, 
         check_ptr(out2, cplx_bytes(dtype), "out2");
         if (out1 == out2) fail(GFFT_ERR_ALIAS, "out1 and out2 must differ");
         check_cuda(launch_separate2x(dtype, in, out1, out2, n, (cudaStream_t)stream), "separate");
+    });
+}
+
+// ---- ragged batches --------------------------------------------------------
+
+gfft_status gfft_ragged_create(gfft_ragged *plan, int dtype, const long long *sizes, long long count)
+{
+    GFFT_GUARD({
+        if (!plan || !sizes) fail(GFFT_ERR_INVALID_VALUE, "NULL argument");
+        *plan = nullptr;
+        check_device();
+        *plan = reinterpret_cast<gfft_ragged>(ragged_create(dtype, sizes, count));
+    });
+}
+
+gfft_status gfft_ragged_destroy(gfft_ragged plan)
+{
+    GFFT_GUARD({
+        if (!plan) fail(GFFT_ERR_INVALID_PLAN, "NULL ragged plan");
+        ragged_destroy(reinterpret_cast<RaggedPlan *>(plan));
+    });
+}
+
+gfft_status gfft_ragged_exec(gfft_ragged plan, int inverse, void *out, const void *in, void *stream)
+{
+    GFFT_GUARD({
+        if (!plan) fail(GFFT_ERR_INVALID_PLAN, "NULL ragged plan");
+        ragged_exec(*reinterpret_cast<RaggedPlan *>(plan), inverse != 0, out, in, (cudaStream_t)stream, true);
+    });
+}
+
+gfft_status gfft_ragged_exec_adjoint(gfft_ragged plan, int inverse, void *out, const void *in, void *stream)
+{
+    GFFT_GUARD({
+        if (!plan) fail(GFFT_ERR_INVALID_PLAN, "NULL ragged plan");
+        ragged_exec(*reinterpret_cast<RaggedPlan *>(plan), inverse == 0, out, in, (cudaStream_t)stream, true);
+    });
+}
+
+gfft_status gfft_ragged_autotune(gfft_ragged plan, void *out, const void *in, void *stream, int *params,
+                                 double *ms)
+{
+    GFFT_GUARD({
+        if (!plan) fail(GFFT_ERR_INVALID_PLAN, "NULL ragged plan");
+        int best[3] = {0, 0, 0};
+        const double t = ragged_autotune(*reinterpret_cast<RaggedPlan *>(plan), out, in, (cudaStream_t)stream, best);
+        if (params) params[0] = best[0], params[1] = best[1], params[2] = best[2];
+        if (ms) *ms = t;
+    });
+}
+
+gfft_status gfft_ragged_elements(gfft_ragged plan, long long *elements)
+{
+    GFFT_GUARD({
+        if (!plan || !elements) fail(GFFT_ERR_INVALID_VALUE, "NULL argument");
+        *elements = ragged_total(reinterpret_cast<RaggedPlan *>(plan));
     });
 }
 

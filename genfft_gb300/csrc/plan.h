@@ -105,6 +105,14 @@ cudaError_t launch_interleave(int dtype, const void *a, long long lda, const voi
                               long long ldz, long long rows, long long cols, cudaStream_t st);
 cudaError_t launch_bitrev_swap(int dtype, void *x, int logn, long long batch, long long dist, cudaStream_t st);
 
+// ---- ragged batches (ragged.cu) ------------------------------------------
+struct RaggedPlan;
+RaggedPlan *ragged_create(int dtype, const long long *sizes, long long count);
+void ragged_destroy(RaggedPlan *p);
+long long ragged_total(const RaggedPlan *p);
+void ragged_exec(RaggedPlan &p, int inverse, void *out, const void *in, cudaStream_t st, bool use_graph);
+double ragged_autotune(RaggedPlan &p, void *out, const void *in, cudaStream_t st, int *best);
+
 }  // namespace gfft
 
 // the public handle

@@ -181,6 +181,28 @@ gfft_status gfft_separate_2x_real_fft(int dtype, int n, void *out1, void *out2, 
 gfft_status gfft_fft_transform_noalloc(int dtype, int n, long long batch, int inverse, void *out,
                                        const void *in, void *stream);
 
+/* ---- ragged batches (no counterpart in the reference, which plans one
+ * size per FFT<T> object, fft.h:56-113) ----------------------------------
+ * `count` fp32 C2C transforms of power-of-two sizes 1 .. 2^18 packed back to
+ * back (transform i starts at the sum of the earlier sizes).  One exec is
+ * one CUDA-graph replay of a single persistent kernel; the graph is
+ * captured on the first exec with a given (in, out, direction).  The plan
+ * owns scratch for its transforms above 2^12 points. */
+typedef struct gfft_ragged_s *gfft_ragged;
+gfft_status gfft_ragged_create(gfft_ragged *plan, int dtype, const long long *sizes, long long count);
+gfft_status gfft_ragged_destroy(gfft_ragged plan);
+gfft_status gfft_ragged_exec(gfft_ragged plan, int inverse, void *out, const void *in, void *stream);
+/* adjoint of direction `inverse` (the conjugate-direction transform) */
+gfft_status gfft_ragged_exec_adjoint(gfft_ragged plan, int inverse, void *out, const void *in, void *stream);
+/* Times the candidate schedules on these buffers and keeps the fastest;
+ * params = {transform passes per work item, CTAs per SM (0 = occupancy),
+ * large transforms first}; *ms = its time.  With GFFT_AUTOTUNE_CACHE set
+ * the choice is cached in that file per size histogram. */
+gfft_status gfft_ragged_autotune(gfft_ragged plan, void *out, const void *in, void *stream, int *params,
+                                 double *ms);
+/* total complex elements of the packed batch */
+gfft_status gfft_ragged_elements(gfft_ragged plan, long long *elements);
+
 /* Device-side error status of this device's kernels since the last call
  * (synchronous): *code = 0 and GFFT_OK if none; otherwise the recorded
  * code (1 = a bounded TMA wait gave up) and GFFT_ERR_TIMEOUT.  Reading
