@@ -332,6 +332,13 @@ def run_reference(args):
     return 0
 
 
+def kernel_name(G, kind, dtype, n0):
+    """The dominant kernel of one exec of the workload."""
+    if kind == "c2c":
+        return "k_c2c_fused" if n0 <= G.max_fused_size(G.F32 if dtype == "f32" else G.F64) else "k_fourstep"
+    return "plan kernels"
+
+
 def make_case(G, torch, kind, dtype, n0, n1, batch, rank):
     """Inputs, outputs, plan and the per-step exec list for one workload."""
     rdt = torch.float32 if dtype == "f32" else torch.float64
@@ -604,7 +611,7 @@ def run_ours(args):
                          "frac": round(achieved / peak, 4), "traffic": traffic,
                          "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)" if peak_src == "measured"
                          else "fallback 6800 GB/s",
-                         "kernel": "k_c2c_fused" if (kind == "c2c" and launches_per_exec == 1) else "plan kernels",
+                         "kernel": kernel_name(G, kind, dtype, n0),
                          "launches_per_exec": launches_per_exec, "avg_exec_ms": round(avg_exec_ms, 5),
                          "avg_launch_ms": round(avg_launch_ms, 5),
                          "algorithmic_bytes_per_exec": batch * per_transform},

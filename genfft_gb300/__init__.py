@@ -176,6 +176,11 @@ class Plan:
             pass
 
 
+def max_fused_size(dtype: int = F32) -> int:
+    """Largest n one fused single-kernel transform handles for dtype."""
+    return int(lib().gfft_max_fused_size(dtype))
+
+
 def device_error() -> int:
     """Read and reset the device error word (0 = no device-side timeout)."""
     code = _I()

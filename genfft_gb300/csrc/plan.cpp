@@ -49,16 +49,6 @@ void C2CCore::init(int dtype_, int logn_, long long batch_hint)
     // N = A * B, A = column-FFT length, B = row-FFT length, both <= 2^12
     logA = logn / 2;
     logB = logn - logA;
-    const int maxc = (int)env_ll("GFFT_TILE_MAXC", 16);
-    ccol = tile_widest(dtype, TILE_COL_TW4, logA, maxc);
-    crow = tile_widest(dtype, TILE_ROW_XPOSE, logB, maxc);
-    if (!ccol || !crow) fail(GFFT_ERR_UNSUPPORTED, "no tile kernel for this length");
-    kcol = tile_find(dtype, TILE_COL_TW4, logA, ccol);
-    krow = tile_find(dtype, TILE_ROW_XPOSE, logB, crow);
-    tw_col = tile_table(dtype, kcol, logA, ccol);
-    tw_row = tile_table(dtype, krow, logB, crow);
-    // inter-pass twiddle W_N^e = tw_hi[e >> lo_bits] * tw_lo[e & (2^lo_bits - 1)]
-    lo_bits = (logn + 1) / 2;
     const long long N = 1LL << logn;
     const int d = dtype;
     auto fill = [d, N](long long count, long long mul) {
@@ -69,9 +59,65 @@ void C2CCore::init(int dtype_, int logn_, long long batch_hint)
             }
         };
     };
+    // inter-pass twiddle W_N^e = tw_hi[e >> lo_bits] * tw_lo[e & (2^lo_bits - 1)]
+    lo_bits = (logn + 1) / 2;
     const std::string key = "4s/" + std::to_string(dtype) + "/" + std::to_string(logn);
     tw_lo = cached_table(key + "/lo", dtype, 1LL << lo_bits, fill(1LL << lo_bits, 1));
     tw_hi = cached_table(key + "/hi", dtype, N >> lo_bits, fill(N >> lo_bits, 1LL << lo_bits));
+
+    // the two-launch tile path: always set up (the persistent kernel needs
+    // 16-byte aligned inputs for its tensor copies and uses it otherwise)
+    const int maxc = (int)env_ll("GFFT_TILE_MAXC", 16);
+    ccol = tile_widest(dtype, TILE_COL_TW4, logA, maxc);
+    crow = tile_widest(dtype, TILE_ROW_XPOSE, logB, maxc);
+    if (!ccol || !crow) fail(GFFT_ERR_UNSUPPORTED, "no tile kernel for this length");
+    kcol = tile_find(dtype, TILE_COL_TW4, logA, ccol);
+    krow = tile_find(dtype, TILE_ROW_XPOSE, logB, crow);
+    tw_col = tile_table(dtype, kcol, logA, ccol);
+    tw_row = tile_table(dtype, krow, logB, crow);
+
+    int nvar = 0;
+    const FourStepKernel *const *vars = fourstep_variants(dtype, logn, &nvar);
+    // the persistent kernel is the faster one for fp32 up to 2^18 points
+    // (measured); above that, and for fp64, the tile launches are
+    const bool fs_default = dtype == GFFT_F32 && logn <= 18;
+    if (nvar > 0 && env_ll("GFFT_FS", fs_default ? 1 : 0) != 0) {
+        // persistent four-step: the widest tile of 64-byte runs or more
+        // that keeps three CTAs per SM, else the widest tile (or the tile
+        // width / stage count GFFT_FS_CC / GFFT_FS_NS name)
+        fs = vars[0];
+        const long long want_cc = env_ll("GFFT_FS_CC", 0), want_ns = env_ll("GFFT_FS_NS", 0);
+        if (want_cc || want_ns) {
+            for (int i = 0; i < nvar; i++)
+                if ((!want_cc || vars[i]->cc == want_cc) && (!want_ns || vars[i]->ns == want_ns)) {
+                    fs = vars[i];
+                    break;
+                }
+        } else {
+            for (int i = 0; i < nvar; i++)
+                if (vars[i]->smem <= 75 * 1024 && vars[i]->cc * (int)cplx_bytes(dtype) >= 64 &&
+                    vars[i]->cr * (int)cplx_bytes(dtype) >= 64) {
+                    fs = vars[i];
+                    break;
+                }
+        }
+        const int l_a = fs->la, l_b = fs->lb;
+        const FourStepKernel *k = fs;
+        tw_a = cached_table("fs/" + std::to_string(d) + "/" + std::to_string(l_a) + "/" + std::to_string(k->twa), d,
+                            k->twa, [k](void *buf) { k->fill_a(buf); });
+        tw_b = cached_table("fs/" + std::to_string(d) + "/" + std::to_string(l_b) + "/" + std::to_string(k->twb), d,
+                            k->twb, [k](void *buf) { k->fill_b(buf); });
+        fs_grid = fourstep_grid(*fs);
+        fourstep_schedule((size_t)N * cplx_bytes(dtype), std::max<long long>(1, batch_hint), fs_grid, fs->ns + 1,
+                          fs->nc + fs->nr, &fs_slots, &fs_lag);
+        group = fs_slots;  // the tile path reuses the ring as its workspace
+        ws_bytes = (size_t)fs_slots * (size_t)N * cplx_bytes(dtype);
+        check_cuda(cudaMalloc(&ws, ws_bytes), "cudaMalloc(workspace)");
+        check_cuda(cudaMalloc(&fs_ctr, (size_t)(2 + 2 * fs_slots) * sizeof(int)), "cudaMalloc(counters)");
+        device_error_word();  // allocated now, never inside a stream capture
+        algo = 3;
+        return;
+    }
     // transforms per launch pair, bounded by the workspace budget
     const long long budget = env_ll("GFFT_WS_BUDGET_MB", 512) << 20;
     group = std::max<long long>(1, budget / (N * (long long)cplx_bytes(dtype)));
@@ -84,12 +130,21 @@ void C2CCore::init(int dtype_, int logn_, long long batch_hint)
 void C2CCore::release()
 {
     if (ws) cudaFree(ws);
+    if (fs_ctr) cudaFree(fs_ctr);
     ws = nullptr;
+    fs_ctr = nullptr;
+}
+
+// transforms per persistent launch: the item count stays far below 2^31
+static long long fs_chunk(const FourStepKernel &k, int lag)
+{
+    return std::max<long long>(1, (1LL << 30) / (k.nc + k.nr) - lag);
 }
 
 int C2CCore::launches(long long batch) const
 {
     if (algo == 1) return 1;
+    if (algo == 3) return (int)((batch + fs_chunk(*fs, fs_lag) - 1) / fs_chunk(*fs, fs_lag));
     return 2 * (int)((batch + group - 1) / group);
 }
 
@@ -103,6 +158,45 @@ void C2CCore::run(int inverse, const void *in, void *out, long long batch, long 
     }
     if (istride != 1 || ostride != 1)
         fail(GFFT_ERR_UNSUPPORTED, "lengths above the fused limit need unit element strides");
+    if (algo == 3) {
+        const size_t eb = cplx_bytes(dtype);
+        const long long chunk = fs_chunk(*fs, fs_lag);
+        const long long A = 1LL << fs->la, B = 1LL << fs->lb;
+        const unsigned units = (unsigned)(eb / 8);
+        bool launched = false;
+        for (long long b0 = 0; b0 < batch; b0 += chunk) {
+            const long long nb = std::min(chunk, batch - b0);
+            FourStepArgs a;
+            a.in = static_cast<const char *>(in) + (size_t)(b0 * idist) * eb;
+            a.out = static_cast<char *>(out) + (size_t)(b0 * odist) * eb;
+            // the input as [batch][A rows][B columns] of 8-byte units
+            CUtensorMap map;
+            if (!make_tensor_map_3d(&map, a.in, (unsigned long long)B * units, (unsigned long long)A,
+                                    (unsigned long long)nb, (unsigned long long)(B * eb),
+                                    (unsigned long long)((nb > 1 ? idist : A * B) * eb), (unsigned)(fs->cc * units),
+                                    (unsigned)fs->boxr)) {
+                if (launched) fail(GFFT_ERR_ALIGN, "input chunk not 16-byte aligned");
+                break;  // unaligned input: the tile path below
+            }
+            a.ws = ws;
+            a.batch = nb;
+            a.idist = idist;
+            a.odist = odist;
+            a.ctr = fs_ctr;
+            a.err = device_error_word();
+            a.tw_a = tw_a;
+            a.tw_b = tw_b;
+            a.tw_lo = tw_lo;
+            a.tw_hi = tw_hi;
+            a.lo_bits = lo_bits;
+            a.slots = fs_slots;
+            a.lag = fs_lag;
+            a.nitems = (int)((nb + fs_lag) * (fs->nc + fs->nr));
+            check_cuda(launch_fourstep(*fs, inverse, map, a, fs_grid, st), "launch persistent four-step");
+            launched = true;
+        }
+        if (launched) return;
+    }
     const long long A = 1LL << logA, B = 1LL << logB, N = A * B;
     const size_t eb = cplx_bytes(dtype);
     const unsigned nmask = (unsigned)(N - 1);

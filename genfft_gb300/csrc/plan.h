@@ -7,6 +7,7 @@
 #include <mutex>
 
 #include "internal.h"
+#include "fourstep.h"
 #include "tiles_registry.h"
 
 namespace gfft {
@@ -19,13 +20,18 @@ bool is_pow2(long long n);
 // memory limit, else the four-step column + row passes through a workspace.
 struct C2CCore {
     int dtype = 0, logn = 0;
-    int algo = 0;  // 1 fused, 2 four-step
+    int algo = 0;  // 1 fused, 2 four-step tile launches, 3 persistent four-step
     const void *tw = nullptr;
+    // persistent four-step: kernel, ring of `fs_slots` transforms, counters
+    const FourStepKernel *fs = nullptr;
+    int fs_slots = 0, fs_lag = 0, fs_grid = 0;
+    int *fs_ctr = nullptr;
+    const void *tw_a = nullptr, *tw_b = nullptr;
     int logA = 0, logB = 0, ccol = 0, crow = 0, lo_bits = 0;
     const TileKernel *kcol = nullptr, *krow = nullptr;
     const void *tw_col = nullptr, *tw_row = nullptr, *tw_lo = nullptr, *tw_hi = nullptr;
     long long group = 0;       // transforms per column/row launch pair
-    void *ws = nullptr;        // group * n elements
+    void *ws = nullptr;        // group * n (algo 2) or fs_slots * n (algo 3) elements
     size_t ws_bytes = 0;
 
     void init(int dtype, int logn, long long batch_hint);

@@ -65,7 +65,18 @@ struct StockhamPlan {
 //   tw  : the plan's twiddle table (StockhamPlan::TW elements)
 // SYNC() must synchronise every thread that shares the shared memory (the
 // whole CTA, or the group).
-template <typename T, int LOGN, int E_, bool INV, typename At, typename Sync>
+// twiddle loads through the read-only cache (tables in global memory)
+struct TwGlobal {
+    template <typename T>
+    __device__ __forceinline__ cpx<T> operator()(const cpx<T> *p) const { return ldg_c(p); }
+};
+// plain loads (tables staged in shared memory)
+struct TwShared {
+    template <typename T>
+    __device__ __forceinline__ cpx<T> operator()(const cpx<T> *p) const { return *p; }
+};
+
+template <typename T, int LOGN, int E_, bool INV, typename TwLoad = TwGlobal, typename At, typename Sync>
 __device__ __forceinline__ void stockham_run(cpx<T> (&v)[StockhamPlan<T, LOGN, E_>::E], int t,
                                              At at, const cpx<T> *__restrict__ tw, Sync SYNC)
 {
@@ -100,7 +111,7 @@ __device__ __forceinline__ void stockham_run(cpx<T> (&v)[StockhamPlan<T, LOGN, E
         const int jm = t % Ns;  // Ns <= G, so j = t
         const cpx<T> *twp = tw + off + jm;
 #pragma unroll
-        for (int r = 1; r < E; r++) v[r] = twmul<INV>(v[r], ldg_c(twp + (r - 1) * Ns));
+        for (int r = 1; r < E; r++) v[r] = twmul<INV>(v[r], TwLoad{}(twp + (r - 1) * Ns));
         dft<E, INV, T>(v);
         if constexpr (p < P - 1) {
             SYNC();

@@ -109,6 +109,20 @@ long long persistent_grid(const void *fn, int threads, size_t smem, long long wo
 
 }  // namespace
 
+bool make_tensor_map_3d(CUtensorMap *map, const void *base, unsigned long long dx, unsigned long long dy,
+                        unsigned long long dz, unsigned long long sy_bytes, unsigned long long sz_bytes, unsigned bx,
+                        unsigned by)
+{
+    if (!encode_fn() || !aligned16(base) || sy_bytes % 16 || sz_bytes % 16) return false;
+    cuuint64_t gdim[3] = {(cuuint64_t)dx, (cuuint64_t)dy, (cuuint64_t)dz};
+    cuuint64_t gstride[2] = {(cuuint64_t)sy_bytes, (cuuint64_t)sz_bytes};
+    cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)by, 1};
+    cuuint32_t estr[3] = {1, 1, 1};
+    return encode_fn()(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, const_cast<void *>(base), gdim, gstride, box, estr,
+                       CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                       CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 unsigned *device_error_word()
 {
     static std::mutex mu;

@@ -3,6 +3,7 @@
 // log2 length, columns per tile).
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstddef>
@@ -49,6 +50,13 @@ cudaError_t launch_colpass(const TileKernel &k, int inverse, long long tiles, lo
 cudaError_t launch_rowpass(const TileKernel &k, int inverse, long long tiles, long long nbatch,
                            const void *in, void *out, long long nrows, long long ld_in, long long ostride,
                            long long idist, long long odist, const void *tw, cudaStream_t st);
+
+// 3D tiled tensor map over 8-byte units (dims x, y, z; byte strides of y
+// and z; box bx x by x 1); false if the driver entry point is missing or
+// the base / strides are not 16-byte aligned
+bool make_tensor_map_3d(CUtensorMap *map, const void *base, unsigned long long dx, unsigned long long dy,
+                        unsigned long long dz, unsigned long long sy_bytes, unsigned long long sz_bytes, unsigned bx,
+                        unsigned by);
 
 // the device error word the persistent kernels report timeouts into
 unsigned *device_error_word();
