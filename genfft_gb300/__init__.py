@@ -14,7 +14,7 @@ from __future__ import annotations
 import ctypes
 import os
 
-__all__ = ["GFFTError", "Plan", "lib", "lib_path", "fft", "ifft", "fft_no_scramble", "rfft", "fft_real_input",
+__all__ = ["GFFTError", "Plan", "lib", "lib_path", "fft", "fft_tc", "ifft", "fft_no_scramble", "rfft", "fft_real_input",
            "fft_interleave", "separate_2x", "dit", "fft_vert", "fft_vert_no_scramble", "fft2", "rfft2",
            "rfft2_2x", "F32", "F64"]
 
@@ -24,6 +24,7 @@ _LIB_PATH = os.path.join(_HERE, "libgenfft_gb300.so")
 F32, F64 = 0, 1
 KIND_C2C, KIND_R2C, KIND_C2C_2D, KIND_R2C_2D, KIND_VERT = 0, 1, 2, 3, 4
 FLAG_HALF_SPECTRUM, FLAG_BITREV_INPUT = 0x1, 0x2
+MODE_PLAIN, MODE_TC_FP16, MODE_TC_BF16 = 0, 1, 2
 
 _STATUS = {
     0: "GFFT_OK", 1: "GFFT_ERR_INVALID_SIZE", 2: "GFFT_ERR_INVALID_VALUE", 3: "GFFT_ERR_ALIAS",
@@ -211,6 +212,28 @@ def fft(x, inverse: bool = False, out=None):
     _check(lib().gfft_fft_transform(_dtype_code(x), n, batch, int(inverse), out.data_ptr(),
                                     x.data_ptr(), _stream_ptr()))
     return out
+
+
+_TC_PLANS = {}
+
+
+def fft_tc(x, inverse: bool = False, mode: int = MODE_TC_FP16, out=None):
+    """Batched fp32 C2C over the last dimension (n = 256, 4096 or 65536) on
+    the split-precision tensor-core path (mode MODE_TC_FP16 or MODE_TC_BF16).
+    Same conventions as fft(): unscaled inverse."""
+    import torch
+    _check_cuda_tensor(x)
+    if x.dtype != torch.complex64:
+        raise TypeError("fft_tc expects complex64")
+    n = x.shape[-1]
+    batch = x.numel() // n
+    key = (x.device.index, n, batch, mode)
+    p = _TC_PLANS.get(key)
+    if p is None:
+        p = _TC_PLANS[key] = Plan(KIND_C2C, F32, n, 0, batch, mode=mode)
+    if out is None:
+        out = torch.empty_like(x)
+    return p.exec(out, x, inverse)
 
 
 def ifft(x, out=None):

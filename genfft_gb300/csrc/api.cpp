@@ -90,7 +90,14 @@ static void validate_desc(const gfft_desc &d)
 {
     if (d.kind < GFFT_KIND_C2C || d.kind > GFFT_KIND_VERT) fail(GFFT_ERR_INVALID_VALUE, "unknown transform kind");
     if (d.dtype != GFFT_F32 && d.dtype != GFFT_F64) fail(GFFT_ERR_INVALID_VALUE, "dtype must be GFFT_F32 or GFFT_F64");
-    if (d.mode != GFFT_MODE_PLAIN) fail(GFFT_ERR_INVALID_VALUE, "unknown mode");
+    if (d.mode != GFFT_MODE_PLAIN && d.mode != GFFT_MODE_TC_FP16 && d.mode != GFFT_MODE_TC_BF16)
+        fail(GFFT_ERR_INVALID_VALUE, "unknown mode");
+    if (d.mode != GFFT_MODE_PLAIN) {
+        if (d.kind != GFFT_KIND_C2C || d.dtype != GFFT_F32 || (d.flags & GFFT_FLAG_BITREV_INPUT))
+            fail(GFFT_ERR_UNSUPPORTED, "tensor-core modes cover fp32 C2C in natural order");
+        if (d.n0 != 256 && d.n0 != 4096 && d.n0 != 65536)
+            fail(GFFT_ERR_UNSUPPORTED, "tensor-core modes cover n = 256, 4096 and 65536");
+    }
     if (d.batch < 1) fail(GFFT_ERR_INVALID_SIZE, "batch must be >= 1");
     if (!is_pow2(d.n0)) fail(GFFT_ERR_INVALID_SIZE, "size must be a power of two >= 1 (README.txt:10-11)");
     if (d.kind == GFFT_KIND_C2C_2D || d.kind == GFFT_KIND_R2C_2D) {
@@ -185,6 +192,11 @@ static gfft_plan_s *make_plan(const gfft_desc &in)
     try {
         switch (d.kind) {
         case GFFT_KIND_C2C:
+            if (d.mode != GFFT_MODE_PLAIN) {
+                p->tc.init(d.mode, ilog2ll(d.n0), d.batch);
+                p->launches = p->tc.launches(d.batch);
+                break;
+            }
             p->c2c.init(d.dtype, ilog2ll(d.n0), d.batch);
             p->launches = p->c2c.launches(d.batch) + (bitrev ? 1 : 0);
             break;
@@ -212,6 +224,7 @@ static gfft_plan_s *make_plan(const gfft_desc &in)
         p->c2c.release();
         p->r2c.release();
         p->c2r.release();
+        p->tc.release();
         throw;
     }
     return p.release();
@@ -259,6 +272,8 @@ static void exec_plan(gfft_plan_s &p, int inverse, void *out, const void *in, co
                            "copy");
             check_cuda(launch_bitrev_swap(d.dtype, out, p.c2c.logn, L.batch, L.odist, st), "bit reversal");
             p.c2c.run(inverse, out, out, L.batch, L.odist, L.odist, 1, 1, st);
+        } else if (d.mode != GFFT_MODE_PLAIN) {
+            p.tc.run(inverse, in, out, L.batch, L.idist, L.odist, L.istride, L.ostride, st);
         } else {
             p.c2c.run(inverse, in, out, L.batch, L.idist, L.odist, L.istride, L.ostride, st);
         }
@@ -394,6 +409,15 @@ static void exec_host(gfft_plan_s &p, int inverse, void *out, const void *in)
         p.stage_bytes_in = per * ib;
         p.stage_bytes_out = per * ob;
     }
+    if (!p.compute_stream) {
+        check_cuda(cudaStreamCreateWithFlags(&p.compute_stream, cudaStreamNonBlocking), "stream");
+        for (int i = 0; i < 3; i++) {
+            check_cuda(cudaEventCreateWithFlags(&p.ev_in[i], cudaEventDisableTiming), "event");
+            check_cuda(cudaEventCreateWithFlags(&p.ev_done[i], cudaEventDisableTiming), "event");
+        }
+    }
+    // copies overlap on three streams; the transforms run in order on one
+    // compute stream, because a plan's workspace serves one exec at a time
     const unsigned char *hin = static_cast<const unsigned char *>(in);
     unsigned char *hout = static_cast<unsigned char *>(out);
     int c = 0;
@@ -402,9 +426,13 @@ static void exec_host(gfft_plan_s &p, int inverse, void *out, const void *in)
         const int s = c % 3;
         cudaStream_t st = p.host_streams[s];
         check_cuda(cudaMemcpyAsync(p.stage[s], hin + b0 * ib, nb * ib, cudaMemcpyHostToDevice, st), "H2D");
+        check_cuda(cudaEventRecord(p.ev_in[s], st), "event");
+        check_cuda(cudaStreamWaitEvent(p.compute_stream, p.ev_in[s], 0), "event wait");
         Layout L = plan_layout(p);
         L.batch = nb;
-        exec_plan(p, inverse, p.stage_out[s], p.stage[s], L, st);
+        exec_plan(p, inverse, p.stage_out[s], p.stage[s], L, p.compute_stream);
+        check_cuda(cudaEventRecord(p.ev_done[s], p.compute_stream), "event");
+        check_cuda(cudaStreamWaitEvent(st, p.ev_done[s], 0), "event wait");
         check_cuda(cudaMemcpyAsync(hout + b0 * ob, p.stage_out[s], nb * ob, cudaMemcpyDeviceToHost, st), "D2H");
     }
     for (int i = 0; i < 3; i++) check_cuda(cudaStreamSynchronize(p.host_streams[i]), "sync");
@@ -416,10 +444,14 @@ static void destroy_plan(gfft_plan_s *p)
         if (p->stage[i]) cudaFree(p->stage[i]);
         if (p->stage_out[i]) cudaFree(p->stage_out[i]);
         if (p->host_streams[i]) cudaStreamDestroy(p->host_streams[i]);
+        if (p->ev_in[i]) cudaEventDestroy(p->ev_in[i]);
+        if (p->ev_done[i]) cudaEventDestroy(p->ev_done[i]);
     }
+    if (p->compute_stream) cudaStreamDestroy(p->compute_stream);
     p->c2c.release();
     p->r2c.release();
     p->c2r.release();
+    p->tc.release();
     p->magic = 0;
     delete p;
 }
@@ -537,7 +569,7 @@ gfft_status gfft_plan_workspace_size(gfft_plan plan, size_t *bytes)
     GFFT_GUARD({
         if (!bytes) fail(GFFT_ERR_INVALID_VALUE, "NULL argument");
         gfft_plan_s *p = checked(plan);
-        *bytes = p->c2c.ws_bytes + p->r2c.c2c.ws_bytes;
+        *bytes = p->c2c.ws_bytes + p->r2c.c2c.ws_bytes + p->tc.ws_bytes;
     });
 }
 

@@ -82,6 +82,22 @@ struct C2RCore {
              cudaStream_t st) const;
 };
 
+// Split-precision tensor-core C2C (tc.cu): fp32 data, radix-16 DFT blocks
+// as FP16 hi+lo or BF16 hi+mid+lo products on tcgen05; n = 256, 4096, 65536
+struct TCCore {
+    int mode = 0, logn = 0;
+    const void *bmat[2] = {nullptr, nullptr};  // DFT-16 split terms, forward / inverse
+    const void *tw256 = nullptr, *tw4096 = nullptr, *twN = nullptr;
+    long long group = 0;  // transforms per column/row launch pair (n = 65536)
+    void *ws = nullptr;
+    size_t ws_bytes = 0;
+    void init(int mode, int logn, long long batch_hint);
+    void release();
+    int launches(long long batch) const;
+    void run(int inverse, const void *in, void *out, long long batch, long long idist, long long odist,
+             long long istride, long long ostride, cudaStream_t st) const;
+};
+
 // ---- kernels in real.cu --------------------------------------------------
 int r2c_fused_max_logh(int dtype);
 size_t r2c_twiddle_count(int dtype, int logh);
@@ -131,10 +147,13 @@ struct gfft_plan_s {
     gfft::ColCore col;   // 2D column pass; VERT
     gfft::R2CCore r2c;   // R2C; real-2D row pass
     gfft::C2RCore c2r;   // C2R; adjoint of R2C
+    gfft::TCCore tc;     // C2C in a tensor-core mode
     // host-path staging (owned, lazily allocated)
     std::mutex host_mu;
     void *stage[3] = {nullptr, nullptr, nullptr};
     void *stage_out[3] = {nullptr, nullptr, nullptr};
     size_t stage_bytes_in = 0, stage_bytes_out = 0;
-    cudaStream_t host_streams[3] = {nullptr, nullptr, nullptr};
+    cudaStream_t host_streams[3] = {nullptr, nullptr, nullptr};  // copies
+    cudaStream_t compute_stream = nullptr;                        // transforms, in order
+    cudaEvent_t ev_in[3] = {nullptr, nullptr, nullptr}, ev_done[3] = {nullptr, nullptr, nullptr};
 };

@@ -15,7 +15,7 @@ namespace gfft {
 // context usable if a copy never lands
 constexpr unsigned long long TMA_WAIT_NS = 1000000000ull;
 
-enum DeviceError : unsigned { DEV_ERR_TMA_TIMEOUT = 1u };
+enum DeviceError : unsigned { DEV_ERR_TMA_TIMEOUT = 1u, DEV_ERR_TC_TIMEOUT = 2u };
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 

@@ -56,7 +56,13 @@ typedef enum gfft_kind {
 } gfft_kind;
 
 typedef enum gfft_mode {
-    GFFT_MODE_PLAIN = 0    /* FP32/FP64 CUDA-core arithmetic */
+    GFFT_MODE_PLAIN = 0,   /* FP32/FP64 CUDA-core arithmetic */
+    /* Split-precision tensor-core C2C (fp32 data, GFFT_KIND_C2C, n = 256,
+     * 4096 or 65536, unit strides).  No counterpart in the reference.
+     * Radix-16 DFT blocks run as dense 16-bit products on the tcgen05 tensor
+     * cores with FP32 accumulation; twiddles are compensated fp32 products. */
+    GFFT_MODE_TC_FP16 = 1, /* FP16 hi + lo terms, per-vector power-of-two scaling, 3 products */
+    GFFT_MODE_TC_BF16 = 2  /* BF16 hi + mid + lo terms, 6 products */
 } gfft_mode;
 
 /* gfft_desc.flags */
@@ -81,9 +87,12 @@ typedef struct gfft_desc {
 typedef struct gfft_plan_s *gfft_plan;
 
 /* ---- plan API -------------------------------------------------------- */
-/* Plans are immutable after creation and may be executed concurrently on
- * different streams; each exec uses its own slice of nothing but the plan's
- * read-only tables.  Creation is thread-safe. */
+/* Plans are immutable after creation.  Sizes that run in one kernel (see
+ * gfft_max_fused_size) read nothing but the plan's tables, so their execs may
+ * run concurrently on different streams.  Multi-pass sizes own a workspace
+ * (gfft_plan_workspace_size) that one exec uses at a time: execs of such a
+ * plan must be ordered (one stream, or events); use one plan per stream to
+ * run them concurrently.  Creation is thread-safe. */
 gfft_status gfft_plan_create(gfft_plan *plan, const gfft_desc *desc);
 gfft_status gfft_plan_destroy(gfft_plan plan);
 /* forward (inverse = 0) or unscaled inverse (inverse = 1) on device memory.
@@ -205,8 +214,8 @@ gfft_status gfft_ragged_elements(gfft_ragged plan, long long *elements);
 
 /* Device-side error status of this device's kernels since the last call
  * (synchronous): *code = 0 and GFFT_OK if none; otherwise the recorded
- * code (1 = a bounded TMA wait gave up) and GFFT_ERR_TIMEOUT.  Reading
- * resets it. */
+ * bits (1 = a bounded TMA or dependency wait gave up, 2 = a bounded wait
+ * for tensor-core MMAs gave up) and GFFT_ERR_TIMEOUT.  Reading resets it. */
 gfft_status gfft_device_error(int *code);
 
 const char *gfft_status_string(gfft_status status);

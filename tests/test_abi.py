@@ -58,6 +58,9 @@ def test_version_and_strings(L):
     (64, 1, 5, 0, 0, 2),       # bad dtype
     (64, 1, 0, 9, 0, 2),       # bad mode
     (64, 1, 0, 0, 0x80, 2),    # unknown flag
+    (1024, 1, 0, 1, 0, 8),     # tensor-core FP16 mode: n outside 256 / 4096 / 65536
+    (4096, 1, 1, 2, 0, 8),     # tensor-core BF16 mode: fp64 data
+    (4096, 1, 0, 1, 0x2, 8),   # tensor-core mode with bit-reversed input
 ])
 def test_plan_validation_without_gpu(L, n0, batch, dtype, mode, flags, status):
     import genfft_gb300 as G

@@ -1,0 +1,103 @@
+"""Split-precision tensor-core C2C (tcgen05): radix-16 DFT blocks as FP16
+hi+lo or BF16 hi+mid+lo products with FP32 accumulation.  Oracle: an FP64
+FFT (numpy on complex128).  Inputs follow the tensor-core workload: complex
+values with log-uniform magnitudes in [1e-3, 1e3] and uniform phase.  Bound:
+relative RMS error <= 2e-7 * log2(n), the fp32 bound; the plain fp32 path's
+error on the same inputs is measured beside it."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+MODES = {"fp16": 1, "bf16": 2}
+
+
+def bound(n):
+    return 2e-7 * int(np.log2(n))
+
+
+def logmag(rng, shape):
+    mag = 10.0 ** rng.uniform(-3, 3, shape)
+    ph = rng.uniform(0, 2 * np.pi, shape)
+    return (mag * np.exp(1j * ph)).astype(np.complex64)
+
+
+def rel_rms(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def run(G, x, n, mode, inverse=False):
+    import torch
+    t = torch.from_numpy(x).cuda()
+    p = G.Plan(G.KIND_C2C, G.F32, n, 0, x.shape[0], mode=mode)
+    y = torch.empty_like(t)
+    p.exec(y, t, inverse)
+    torch.cuda.synchronize()
+    return y.cpu().numpy()
+
+
+@pytest.mark.parametrize("mode", sorted(MODES))
+@pytest.mark.parametrize("n,batch", [(256, 37), (4096, 5), (65536, 3)])
+def test_tc_vs_fp64(gfft, n, batch, mode):
+    rng = np.random.default_rng(n + batch)
+    x = logmag(rng, (batch, n))
+    x64 = x.astype(np.complex128)
+    for inv in (False, True):
+        exact = np.fft.ifft(x64) * n if inv else np.fft.fft(x64)
+        got = run(gfft, x, n, MODES[mode], inv)
+        plain = run(gfft, x, n, 0, inv)
+        e_tc, e_plain = rel_rms(got, exact), rel_rms(plain, exact)
+        print(f"n={n} {mode} inv={inv}: tc {e_tc:.3g} plain {e_plain:.3g}")
+        assert e_tc <= bound(n), (n, mode, inv, e_tc)
+        # every transform of the batch, not just the norm over all of them
+        for b in range(batch):
+            assert rel_rms(got[b], exact[b]) <= 2 * bound(n), (n, mode, inv, b)
+
+
+@pytest.mark.parametrize("mode", sorted(MODES))
+def test_tc_round_trip_and_zero(gfft, mode):
+    import torch
+    n, batch = 4096, 4
+    rng = np.random.default_rng(3)
+    x = logmag(rng, (batch, n))
+    x[1] = 0  # an all-zero transform (scale exponent clamp)
+    y = run(gfft, x, n, MODES[mode])
+    assert np.all(y[1] == 0)
+    t = torch.from_numpy(y).cuda()
+    z = gfft.fft_tc(t, True, MODES[mode]).cpu().numpy() / n
+    assert rel_rms(z, x) <= 2 * bound(n)
+
+
+def test_tc_c4_full_size_parseval(gfft):
+    """n = 2^16, batch 4096 (the tensor-core workload): Parseval on every
+    transform and an FP64 comparison on three of them."""
+    import torch
+    n, batch = 1 << 16, 4096
+    g = torch.Generator(device="cuda").manual_seed(4)
+    mag = 10.0 ** (torch.rand(batch, n, device="cuda", generator=g, dtype=torch.float64) * 6 - 3)
+    ph = torch.rand(batch, n, device="cuda", generator=g, dtype=torch.float64) * (2 * np.pi)
+    x = torch.polar(mag, ph).to(torch.complex64)
+    for mode in MODES.values():
+        y = gfft.fft_tc(x, False, mode)
+        px = (x.abs().double() ** 2).sum(-1) * n
+        py = (y.abs().double() ** 2).sum(-1)
+        assert torch.allclose(py, px, rtol=2e-5), mode
+        rows = [0, batch // 2, batch - 1]
+        exact = np.fft.fft(x[rows].cpu().numpy().astype(np.complex128))
+        assert rel_rms(y[rows].cpu().numpy(), exact) <= bound(n), mode
+        del y
+    assert gfft.device_error() == 0
+
+
+def test_tc_adjoint_is_conjugate_direction(gfft):
+    import torch
+    n, batch = 256, 20
+    rng = np.random.default_rng(11)
+    g = logmag(rng, (batch, n))
+    p = gfft.Plan(gfft.KIND_C2C, gfft.F32, n, 0, batch, mode=1)
+    tg = torch.from_numpy(g).cuda()
+    out = torch.empty_like(tg)
+    p.adjoint(out, tg)
+    torch.cuda.synchronize()
+    exact = np.fft.ifft(g.astype(np.complex128)) * n
+    assert rel_rms(out.cpu().numpy(), exact) <= bound(n)
