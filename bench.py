@@ -45,7 +45,17 @@ WORKLOADS = {
     "c2d_f32_4096x4096": ("c2d", "f32", 4096, 4096, 1),
     "r2d_f32_4096x4096": ("r2d", "f32", 4096, 4096, 1),
     "ragged_f32_10000": ("ragged", "f32", 0, 0, 10000),
+    # split-precision tensor-core path (tcgen05), log-uniform magnitudes
+    "tcfp16_f32_65536x4096": ("c2c", "f32", 1 << 16, 0, 4096, 1),
+    "tcbf16_f32_65536x4096": ("c2c", "f32", 1 << 16, 0, 4096, 2),
 }
+MODE_NAMES = {0: "plain", 1: "tc_fp16", 2: "tc_bf16"}
+
+
+def workload(name):
+    """(kind, dtype, n0, n1, batch, mode)"""
+    w = WORKLOADS[name]
+    return w if len(w) == 6 else w + (0,)
 DEFAULT = "c2c_f32_4096x16384"
 
 THROTTLE_BITS = {
@@ -312,7 +322,7 @@ def run_reference(args):
     world, rank, _ = int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), 0
     if rank != 0:
         return 0
-    kind, dtype, n0, n1, batch = WORKLOADS[args.workload]
+    kind, dtype, n0, n1, batch, _ = workload(args.workload)
     steps = max(1, args.steps)
     cb, med, reps = time_cpu(kind, dtype, n0, n1, batch, budget_s=max(5.0, min(60.0, 3.0 * steps)),
                              max_reps=steps)
@@ -332,20 +342,30 @@ def run_reference(args):
     return 0
 
 
-def kernel_name(G, kind, dtype, n0):
+def kernel_name(G, kind, dtype, n0, mode=0):
     """The dominant kernel of one exec of the workload."""
+    if mode:
+        return "k_tc"
     if kind == "c2c":
         return "k_c2c_fused" if n0 <= G.max_fused_size(G.F32 if dtype == "f32" else G.F64) else "k_fourstep"
     return "plan kernels"
 
 
-def make_case(G, torch, kind, dtype, n0, n1, batch, rank):
+def make_case(G, torch, kind, dtype, n0, n1, batch, rank, mode=0):
     """Inputs, outputs, plan and the per-step exec list for one workload."""
     rdt = torch.float32 if dtype == "f32" else torch.float64
     cdt = torch.complex64 if dtype == "f32" else torch.complex128
     dcode = G.F32 if dtype == "f32" else G.F64
     gen = torch.Generator(device="cuda").manual_seed(1234 + rank)
-    if kind == "c2c":
+    if kind == "c2c" and mode:
+        # tensor-core workload: magnitudes log-uniform in [1e-3, 1e3], uniform phase
+        shape_in = shape_out = (batch, n0)
+        mag = 10.0 ** (torch.rand(batch, n0, device="cuda", generator=gen) * 6 - 3)
+        ph = torch.rand(batch, n0, device="cuda", generator=gen) * (2 * math.pi)
+        x = torch.polar(mag, ph)
+        del mag, ph
+        plan = G.Plan(G.KIND_C2C, dcode, n0, 0, batch, mode=mode)
+    elif kind == "c2c":
         shape_in = shape_out = (batch, n0)
         x = torch.randn(*shape_in, dtype=cdt, device="cuda", generator=gen)
         plan = G.Plan(G.KIND_C2C, dcode, n0, 0, batch)
@@ -511,9 +531,9 @@ def run_ours(args):
     world, rank, local = dist_setup()
     dev = local if world > 1 else 0
     torch.cuda.set_device(dev)
-    kind, dtype, n0, n1, batch = WORKLOADS[args.workload]
+    kind, dtype, n0, n1, batch, mode = workload(args.workload)
     G.lib()
-    x, y, z, plan, execs = make_case(G, torch, kind, dtype, n0, n1, batch, rank)
+    x, y, z, plan, execs = make_case(G, torch, kind, dtype, n0, n1, batch, rank, mode)
     launches_per_exec = plan.launches()
     stream = torch.cuda.current_stream()
     sp = stream.cuda_stream
@@ -580,21 +600,54 @@ def run_ours(args):
     d2h = sum(o.numel() * o.element_size() for o, _, _ in hexecs)
 
     # sanity on a few rows: round trip (complex) or the FP64 reference (real)
+    # first and last transforms (a race between chunks would show in the last)
+    rows = [0, batch - 1] if batch > 1 else [0]
     if z is not None:
         npts = n0 * (n1 or 1)
-        check = float(np.max(np.abs(z.reshape(batch, -1)[:2].cpu().numpy() / npts
-                                    - x.reshape(batch, -1)[:2].cpu().numpy())))
-        e2e_check = float(np.max(np.abs(hz.reshape(batch, -1)[:2].numpy() / npts
-                                        - x.reshape(batch, -1)[:2].cpu().numpy())))
+        xr = x.reshape(batch, -1)[rows].cpu().numpy()
+        rel = lambda a: float(np.linalg.norm(a / npts - xr) / np.linalg.norm(xr))  # noqa: E731
+        check = rel(z.reshape(batch, -1)[rows].cpu().numpy())
+        e2e_check = rel(hz.reshape(batch, -1)[rows].numpy())
     else:
-        xs = x[:1].cpu().numpy().astype(np.float64)
+        xs = x[rows].cpu().numpy().astype(np.float64)
         ref = np.fft.rfft2(xs) if kind == "r2d" else np.fft.rfft(xs)
-        check = float(np.linalg.norm(y[:1].cpu().numpy() - ref) / np.linalg.norm(ref))
-        e2e_check = float(np.linalg.norm(hy[:1].numpy() - ref) / np.linalg.norm(ref))
+        check = float(np.linalg.norm(y[rows].cpu().numpy() - ref) / np.linalg.norm(ref))
+        e2e_check = float(np.linalg.norm(hy[rows].numpy() - ref) / np.linalg.norm(ref))
 
+    accuracy = None
+    if mode:
+        rows = [0, batch - 1]
+        xs = x[rows].cpu().numpy().astype(np.complex128)
+        exact = np.fft.fft(xs)
+        err = lambda a: float(np.linalg.norm(a - exact) / np.linalg.norm(exact))  # noqa: E731
+        pp = G.Plan(G.KIND_C2C, G.F32, n0, 0, len(rows))
+        xp = x[rows].contiguous()
+        yp = torch.empty_like(xp)
+        pp.exec(yp, xp)
+        # plain path time on the same full batch, for the tensor-core comparison
+        plain = G.Plan(G.KIND_C2C, G.F32, n0, 0, batch)
+        for _ in range(2):
+            plain.exec(y, x)
+        a_ev, b_ev = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a_ev.record(stream)
+        for _ in range(5):
+            plain.exec(y, x)
+        b_ev.record(stream)
+        torch.cuda.synchronize()
+        plain_ms = a_ev.elapsed_time(b_ev) / 5
+        plan.exec(y, x)
+        torch.cuda.synchronize()
+        accuracy = {"rel_rms_vs_fp64": err(y[rows].cpu().numpy()),
+                    "plain_rel_rms_vs_fp64": err(yp.cpu().numpy()),
+                    "bound": 2e-7 * math.log2(n0), "rows": rows,
+                    "mode": MODE_NAMES[mode], "exec_ms": round(avg_exec_ms, 5),
+                    "plain_exec_ms": round(plain_ms, 5),
+                    "tc_over_plain_time": round(avg_exec_ms / plain_ms, 3)}
+        del plain, pp
     if rank == 0:
         line = {
-            "metric": f"{kind} {dtype} GB/s (algorithmic, HBM-resident)",
+            "metric": f"{kind} {dtype} GB/s (algorithmic, HBM-resident)"
+                      + (f", {MODE_NAMES[mode]} tensor-core path" if mode else ""),
             "value": round(gbs, 2), "unit": "GB/s", "n_gpus": world, "steps": K,
             "warmup": max(3, args.warmup), "ms_per_step": round(ms / K, 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": dtype,
@@ -611,7 +664,7 @@ def run_ours(args):
                          "frac": round(achieved / peak, 4), "traffic": traffic,
                          "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)" if peak_src == "measured"
                          else "fallback 6800 GB/s",
-                         "kernel": kernel_name(G, kind, dtype, n0),
+                         "kernel": kernel_name(G, kind, dtype, n0, mode),
                          "launches_per_exec": launches_per_exec, "avg_exec_ms": round(avg_exec_ms, 5),
                          "avg_launch_ms": round(avg_launch_ms, 5),
                          "algorithmic_bytes_per_exec": batch * per_transform},
@@ -619,7 +672,7 @@ def run_ours(args):
                     "d2h_bytes_per_step": d2h, "api": "gfft_exec_host (pinned host buffers)",
                     "steps": e2e_steps},
             "gpu_launches": E * K * launches_per_exec,
-            "check": check, "e2e_check": e2e_check,
+            "check": check, "e2e_check": e2e_check, "accuracy": accuracy,
             "clocks": clk.summary(),
         }
         if not args.no_cpu:

@@ -22,9 +22,12 @@
 //   FP16: A_hi B_hi + A_lo B_hi + A_hi B_lo             (3 x K=32)
 //   BF16: the six products of total order <= 2         (6 x K=32)
 // against the split 32 x 32 real form of the DFT-16 matrix, accumulating in
-// FP32 in tensor memory (M = 128, N = 32 per half).  Thread m reads its row
-// back with tcgen05.ld, undoes the scale and scatters the 16 outputs to the
-// tile (or to global memory after the last stage).
+// FP32 in tensor memory (M = 128, N = 32 per half): the hi x hi products in
+// one accumulator, the smaller correction products in another, added in FP32
+// on the CUDA cores (the tensor core's accumulator truncates; keeping the
+// large and small terms apart keeps that error at the corrections' scale).
+// Thread m reads its row back with tcgen05.ld, undoes the scale and scatters
+// the 16 outputs to the tile (or to global memory after the last stage).
 //
 // Kinds: K256  - 16 transforms of 256 points per tile (2 stages)
 //        K4096 - one transform of 4096 points per tile (3 stages)
@@ -55,6 +58,7 @@ constexpr int A_HALF = 128 * 64;             // bytes of one 128-row half
 constexpr int B_TERM = 32 * 64;              // bytes: 32 rows x 32 16-bit values
 constexpr int XELEMS = 4096 + 4096 / 16 + 2; // padded tile (spad<float>), even
 constexpr uint32_t LBO = 128, SBO = 512;     // core-matrix strides of both operands
+constexpr uint32_t TMEM_COLS = 128;           // 2 halves x (main + correction) x 32 columns
 
 enum Kind { K256 = 0, K4096 = 1, KCOL = 2, KROW = 3 };
 
@@ -180,13 +184,15 @@ __global__ void __launch_bounds__(THREADS, Smem<BF16>::MIN_BLOCKS) k_tc(const Tc
         mbar_init(bar, 1);
         fence_barrier_init();
     }
-    if (tid < 32) tc::tmem_alloc(s_taddr, 64);
+    if (tid < 32) tc::tmem_alloc(s_taddr, TMEM_COLS);
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t taddr = *s_taddr;
-    // this thread's accumulator row: lane 32 (warp % 4) + lane, columns 32 * half
-    const uint32_t my_tmem = taddr + ((uint32_t)((tid >> 5) & 3) * 32u << 16) + (uint32_t)(tid >> 7) * 32u;
+    // this thread's accumulator row: lane 32 (warp % 4) + lane; each 128-row
+    // half owns 64 columns: the hi x hi products in the first 32, the
+    // correction products in the next 32
+    const uint32_t my_tmem = taddr + ((uint32_t)((tid >> 5) & 3) * 32u << 16) + (uint32_t)(tid >> 7) * 64u;
     const uint32_t a_s = smem_u32(Aop), b_s = smem_u32(Bop);
     constexpr uint32_t IDESC = tc::idesc_f16(BF16, 128, 32);
     constexpr int S = KIND == K4096 ? 3 : 2;
@@ -256,7 +262,10 @@ __global__ void __launch_bounds__(THREADS, Smem<BF16>::MIN_BLOCKS) k_tc(const Tc
                             const uint64_t ad =
                                 tc::smem_desc(a_s + P::pa(pi) * A_TERM + g * A_HALF + kc * 2 * LBO, LBO, SBO);
                             const uint64_t bd = tc::smem_desc(b_s + P::pb(pi) * B_TERM + kc * 2 * LBO, LBO, SBO);
-                            tc::mma_f16(taddr + (uint32_t)g * 32u, ad, bd, IDESC, pi > 0 || kc > 0);
+                            // hi x hi into the main accumulator, the rest into
+                            // the correction accumulator
+                            const uint32_t d = taddr + (uint32_t)g * 64u + (pi > 0 ? 32u : 0u);
+                            tc::mma_f16(d, ad, bd, IDESC, pi > 1 || kc > 0);
                         }
                     }
                 }
@@ -266,12 +275,20 @@ __global__ void __launch_bounds__(THREADS, Smem<BF16>::MIN_BLOCKS) k_tc(const Tc
             phase ^= 1u;
             if (!ok) break;
             tc::fence_after_sync();
-            float r32[32];
-            tc::tmem_ld32(my_tmem, r32);
-            tc::fence_before_sync();
+            // main + correction, summed in FP32 with round-to-nearest outside
+            // the tensor core (its accumulator does not round to nearest)
             float2 o[16];
+            {
+                float r32[32];
+                tc::tmem_ld32(my_tmem, r32);
 #pragma unroll
-            for (int k = 0; k < 16; k++) o[k] = make_float2(r32[2 * k] * isc, r32[2 * k + 1] * isc);
+                for (int k = 0; k < 16; k++) o[k] = make_float2(r32[2 * k], r32[2 * k + 1]);
+                tc::tmem_ld32(my_tmem + 32u, r32);
+#pragma unroll
+                for (int k = 0; k < 16; k++)
+                    o[k] = make_float2((o[k].x + r32[2 * k]) * isc, (o[k].y + r32[2 * k + 1]) * isc);
+            }
+            tc::fence_before_sync();
 
             // ---- scatter (the gathers of this stage are done: every thread
             // passed the MMA barrier)
@@ -338,7 +355,7 @@ __global__ void __launch_bounds__(THREADS, Smem<BF16>::MIN_BLOCKS) k_tc(const Tc
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
-    if (tid < 32) tc::tmem_dealloc(taddr, 64);
+    if (tid < 32) tc::tmem_dealloc(taddr, TMEM_COLS);
 }
 
 // ---------------------------------------------------------------------------
