@@ -87,7 +87,7 @@ struct C2RCore {
 struct TCCore {
     int mode = 0, logn = 0;
     const void *bmat[2] = {nullptr, nullptr};  // DFT-16 split terms, forward / inverse
-    const void *tw256 = nullptr, *tw4096 = nullptr, *twN = nullptr;
+    const void *tw256 = nullptr, *tw2 = nullptr;  // W_256 and the low-order W_N table
     long long group = 0;  // transforms per column/row launch pair (n = 65536)
     void *ws = nullptr;
     size_t ws_bytes = 0;

@@ -33,6 +33,11 @@
 //        K4096 - one transform of 4096 points per tile (3 stages)
 //        KCOL / KROW - the column and row passes of n = 65536 = 256 x 256
 //        (four-step, W_65536 twiddle after the column pass).
+// Every twiddle comes from two 256-entry (hi, lo) tables in shared memory:
+// W_N^e = W_256^(e >> s) * W_N^(e mod 2^s), two compensated products.
+// Tiles arrive by TMA (bulk copies; a 3D tensor box for KCOL) into a dense
+// stage buffer: the copy of the next tile starts as soon as stage 0 of the
+// current one has gathered its inputs, and lands while the later stages run.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
@@ -47,6 +52,7 @@
 #include "plan.h"
 #include "stockham.cuh"
 #include "tc.cuh"
+#include "tiles_registry.h"
 #include "twiddle.h"
 
 namespace gfft {
@@ -80,10 +86,12 @@ struct Prec<true> {
 template <bool BF16>
 struct Smem {
     static constexpr int B_OFF = Prec<BF16>::TA * A_TERM;
-    static constexpr int X_OFF = B_OFF + Prec<BF16>::TB * B_TERM;
-    static constexpr int T_OFF = X_OFF + XELEMS * 8;     // W_256 (hi, lo) pairs
-    static constexpr int BAR_OFF = T_OFF + 512 * 8;
-    static constexpr int BYTES = BAR_OFF + 16;
+    static constexpr int STG_OFF = B_OFF + Prec<BF16>::TB * B_TERM;  // incoming tile, dense (TMA)
+    static constexpr int X_OFF = STG_OFF + 4096 * 8;                  // inter-stage tile, padded
+    static constexpr int T_OFF = X_OFF + XELEMS * 8;     // W_256^e (hi, lo) pairs
+    static constexpr int T2_OFF = T_OFF + 512 * 8;       // W_N^e, e < 256 (KCOL) / W_4096^e, e < 16 (K4096)
+    static constexpr int BAR_OFF = T2_OFF + 512 * 8;
+    static constexpr int BYTES = BAR_OFF + 24;  // MMA barrier, load barrier, TMEM address
     static constexpr int MIN_BLOCKS = (228 * 1024) / (BYTES + 1024);
 };
 
@@ -93,9 +101,9 @@ struct TcArgs {
     long long ntiles, batch, idist, odist;
     const void *bmat;      // TB split terms of the DFT-16 matrix, canonical layout
     const float2 *tw256;   // W_256^e, (hi, lo) pairs
-    const float2 *tw4096;  // W_4096^e, (hi, lo) pairs (K4096)
-    const float2 *twN;     // W_65536^e, (hi, lo) pairs (KCOL)
+    const float2 *tw2;     // W_4096^e, e < 16 (K4096) or W_65536^e, e < 256 (KCOL): (hi, lo) pairs
     unsigned *err;
+    int tma;  // 1: TMA copies of the tiles (16-byte aligned), 0: thread loads
 };
 
 __device__ __forceinline__ int xpad(int i) { return i + (i >> 4); }
@@ -159,18 +167,44 @@ __device__ __forceinline__ float split_store(const float2 (&v)[16], unsigned cha
     return isc;
 }
 
+// thread 0: start the copy of tile w into the dense stage buffer (TMA)
+template <int KIND>
+__device__ __forceinline__ void issue_tile(const CUtensorMap *map, const TcArgs &a, long long w, float2 *stg,
+                                           uint64_t *tbar)
+{
+    if (KIND == K4096) {
+        mbar_arrive_expect_tx(tbar, 32768u);
+        bulk_load(stg, a.in + w * a.idist, 32768u, tbar);
+    } else if (KIND == K256) {
+        const long long t0 = w * 16;
+        const int valid = (int)(a.batch - t0 < 16 ? a.batch - t0 : 16);
+        mbar_arrive_expect_tx(tbar, (uint32_t)valid * 2048u);
+        for (int sl = 0; sl < valid; sl++) bulk_load(stg + sl * 256, a.in + (t0 + sl) * a.idist, 2048u, tbar);
+    } else if (KIND == KROW) {
+        mbar_arrive_expect_tx(tbar, 32768u);
+        bulk_load(stg, a.in + (w >> 4) * a.idist + (w & 15) * 16 * 256, 32768u, tbar);
+    } else {  // KCOL: 256 rows x 16 columns, one tensor box
+        mbar_arrive_expect_tx(tbar, 32768u);
+        tensor_load_3d(stg, map, (int)((w & 15) * 16), 0, (int)(w >> 4), tbar);
+    }
+}
+
 template <bool BF16, int KIND, bool INV>
-__global__ void __launch_bounds__(THREADS, Smem<BF16>::MIN_BLOCKS) k_tc(const TcArgs a)
+__global__ void __launch_bounds__(THREADS, Smem<BF16>::MIN_BLOCKS)
+    k_tc(const __grid_constant__ CUtensorMap map, const TcArgs a)
 {
     using P = Prec<BF16>;
     using L = Smem<BF16>;
     extern __shared__ __align__(1024) unsigned char sm[];
     unsigned char *const Aop = sm;
     unsigned char *const Bop = sm + L::B_OFF;
+    float2 *const STG = reinterpret_cast<float2 *>(sm + L::STG_OFF);
     float2 *const X = reinterpret_cast<float2 *>(sm + L::X_OFF);
     float2 *const T = reinterpret_cast<float2 *>(sm + L::T_OFF);
+    float2 *const T2 = reinterpret_cast<float2 *>(sm + L::T2_OFF);
     uint64_t *const bar = reinterpret_cast<uint64_t *>(sm + L::BAR_OFF);
-    uint32_t *const s_taddr = reinterpret_cast<uint32_t *>(sm + L::BAR_OFF + 8);
+    uint64_t *const tbar = bar + 1;
+    uint32_t *const s_taddr = reinterpret_cast<uint32_t *>(sm + L::BAR_OFF + 16);
     const int tid = threadIdx.x;
 
     // ---- set-up: DFT matrix terms and W_256 to shared memory, barrier, TMEM
@@ -179,9 +213,14 @@ __global__ void __launch_bounds__(THREADS, Smem<BF16>::MIN_BLOCKS) k_tc(const Tc
         uint4 *dst = reinterpret_cast<uint4 *>(Bop);
         for (int i = tid; i < P::TB * B_TERM / 16; i += THREADS) dst[i] = src[i];
         for (int i = tid; i < 512; i += THREADS) T[i] = a.tw256[i];
+        if (KIND == KCOL)
+            for (int i = tid; i < 512; i += THREADS) T2[i] = a.tw2[i];
+        if (KIND == K4096)
+            for (int i = tid; i < 32; i += THREADS) T2[i] = a.tw2[i];
     }
     if (tid == 0) {
         mbar_init(bar, 1);
+        mbar_init(tbar, 1);
         fence_barrier_init();
     }
     if (tid < 32) tc::tmem_alloc(s_taddr, TMEM_COLS);
@@ -197,38 +236,49 @@ __global__ void __launch_bounds__(THREADS, Smem<BF16>::MIN_BLOCKS) k_tc(const Tc
     constexpr uint32_t IDESC = tc::idesc_f16(BF16, 128, 32);
     constexpr int S = KIND == K4096 ? 3 : 2;
     const int m = tid;
-    uint32_t phase = 0;
+    uint32_t phase = 0, tphase = 0;
     bool ok = true;
+    if (a.tma && tid == 0 && blockIdx.x < a.ntiles) issue_tile<KIND>(&map, a, blockIdx.x, STG, tbar);
 
     for (long long w = blockIdx.x; w < a.ntiles; w += gridDim.x) {
-        // ---- load the tile (coalesced) into X
-        if (KIND == K4096) {
-            const float2 *src = a.in + w * a.idist;
-#pragma unroll 4
-            for (int q = 0; q < 16; q++) X[xpad(tid + 256 * q)] = __ldcs(src + tid + 256 * q);
-        } else if (KIND == K256 || KIND == KROW) {
-#pragma unroll 4
-            for (int q = 0; q < 16; q++) {
-                const int i = tid + 256 * q, sl = i >> 8, pos = i & 255;
-                float2 val = make_float2(0.f, 0.f);
-                if (KIND == K256) {
-                    const long long t = w * 16 + sl;
-                    if (t < a.batch) val = __ldcs(a.in + t * a.idist + pos);
-                } else {
-                    const long long t = w >> 4;
-                    val = __ldcs(a.in + t * a.idist + ((w & 15) * 16 + sl) * 256 + pos);
+        if (a.tma) {
+            // the copy of this tile, started during the previous one
+            ok = __syncthreads_and(mbar_wait(tbar, tphase));
+            tphase ^= 1u;
+            if (!ok) break;
+        } else {
+            // thread loads into the dense stage buffer (all 16 in flight
+            // before the first store)
+            float2 ld[16];
+            if (KIND == K4096) {
+                const float2 *src = a.in + w * a.idist;
+#pragma unroll
+                for (int q = 0; q < 16; q++) ld[q] = __ldcs(src + tid + 256 * q);
+            } else if (KIND == K256 || KIND == KROW) {
+#pragma unroll
+                for (int q = 0; q < 16; q++) {
+                    const int i = tid + 256 * q, sl = i >> 8, pos = i & 255;
+                    ld[q] = make_float2(0.f, 0.f);
+                    if (KIND == K256) {
+                        const long long t = w * 16 + sl;
+                        if (t < a.batch) ld[q] = __ldcs(a.in + t * a.idist + pos);
+                    } else {
+                        const long long t = w >> 4;
+                        ld[q] = __ldcs(a.in + t * a.idist + ((w & 15) * 16 + sl) * 256 + pos);
+                    }
                 }
-                X[xpad(i)] = val;
+            } else {  // KCOL: X[a * 16 + c] = x[a * 256 + c0 + c]
+                const long long t = w >> 4, c0 = (w & 15) * 16;
+#pragma unroll
+                for (int q = 0; q < 16; q++) {
+                    const int i = tid + 256 * q;
+                    ld[q] = __ldcs(a.in + t * a.idist + (i >> 4) * 256 + c0 + (i & 15));
+                }
             }
-        } else {  // KCOL: X[a * 16 + c] = x[a * 256 + c0 + c]
-            const long long t = w >> 4, c0 = (w & 15) * 16;
-#pragma unroll 4
-            for (int q = 0; q < 16; q++) {
-                const int i = tid + 256 * q;
-                X[xpad(i)] = __ldcs(a.in + t * a.idist + (i >> 4) * 256 + c0 + (i & 15));
-            }
+#pragma unroll
+            for (int q = 0; q < 16; q++) STG[tid + 256 * q] = ld[q];
+            __syncthreads();
         }
-        __syncthreads();
 
 #pragma unroll 1
         for (int s = 0; s < S; s++) {
@@ -236,16 +286,24 @@ __global__ void __launch_bounds__(THREADS, Smem<BF16>::MIN_BLOCKS) k_tc(const Tc
             float2 v[16];
             const int base = (KIND == K256 || KIND == KROW) ? (m >> 4) * 256 + (m & 15) : m;
             const int step = (KIND == K256 || KIND == KROW) ? 16 : 256;
+            if (s == 0) {
 #pragma unroll
-            for (int r = 0; r < 16; r++) v[r] = X[xpad(base + step * r)];
+                for (int r = 0; r < 16; r++) v[r] = STG[base + step * r];
+            } else {
+#pragma unroll
+                for (int r = 0; r < 16; r++) v[r] = X[xpad(base + step * r)];
+            }
             if (s == 1) {
                 const int jj = (KIND == KCOL) ? (m >> 4) : (m & 15);  // W_256^(jj r)
 #pragma unroll
                 for (int r = 1; r < 16; r++) v[r] = ctw<INV>(v[r], T[2 * (jj * r)], T[2 * (jj * r) + 1]);
-            } else if (s == 2) {  // K4096 last pass: W_4096^(m r)
+            } else if (s == 2) {  // K4096 last pass: W_4096^(m r) = W_256^(e >> 4) W_4096^(e & 15)
 #pragma unroll
-                for (int r = 1; r < 16; r++)
-                    v[r] = ctw<INV>(v[r], __ldg(a.tw4096 + 2 * (m * r)), __ldg(a.tw4096 + 2 * (m * r) + 1));
+                for (int r = 1; r < 16; r++) {
+                    const int e = m * r;
+                    v[r] = ctw<INV>(ctw<INV>(v[r], T[2 * (e >> 4)], T[2 * (e >> 4) + 1]), T2[2 * (e & 15)],
+                                    T2[2 * (e & 15) + 1]);
+                }
             }
             const float isc = split_store<BF16>(v, Aop, m);
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -270,6 +328,11 @@ __global__ void __launch_bounds__(THREADS, Smem<BF16>::MIN_BLOCKS) k_tc(const Tc
                     }
                 }
                 tc::commit(bar);
+                // every thread has gathered this tile: refill the stage buffer
+                if (s == 0 && a.tma && w + gridDim.x < a.ntiles) {
+                    fence_proxy_async_smem();
+                    issue_tile<KIND>(&map, a, w + gridDim.x, STG, tbar);
+                }
             }
             ok = __syncthreads_and(mbar_wait(bar, phase));
             phase ^= 1u;
@@ -327,9 +390,11 @@ __global__ void __launch_bounds__(THREADS, Smem<BF16>::MIN_BLOCKS) k_tc(const Tc
                     float2 *dst = a.out + t * a.odist + col;
 #pragma unroll
                     for (int k = 0; k < 16; k++) {
+                        // W_65536^e = W_256^(e >> 8) W_65536^(e & 255)
                         const int K = j + 16 * k;
                         const int e = (col * K) & 65535;
-                        dst[(long long)K * 256] = ctw<INV>(o[k], __ldg(a.twN + 2 * e), __ldg(a.twN + 2 * e + 1));
+                        dst[(long long)K * 256] = ctw<INV>(ctw<INV>(o[k], T[2 * (e >> 8)], T[2 * (e >> 8) + 1]),
+                                                           T2[2 * (e & 255)], T2[2 * (e & 255) + 1]);
                     }
                 } else {  // KROW: transpose through X, then 16-element runs
 #pragma unroll
@@ -351,6 +416,7 @@ __global__ void __launch_bounds__(THREADS, Smem<BF16>::MIN_BLOCKS) k_tc(const Tc
     if (!ok) {
         if (tid == 0) atomicOr(a.err, DEV_ERR_TC_TIMEOUT);
         mbar_wait(bar, phase ^ 1u);  // let an MMA still in flight finish (bounded)
+        if (a.tma) mbar_wait(tbar, tphase);  // and a tile copy (bounded)
     }
     tc::fence_before_sync();
     __syncthreads();
@@ -396,10 +462,10 @@ void fill_bmat(bool bf16, bool inv, unsigned char *out)
         }
 }
 
-// W_M^e for e < M as (hi, lo) fp32 pairs
-void fill_pairs(long long M, float *out)
+// W_M^e for e < count as (hi, lo) fp32 pairs
+void fill_pairs(long long M, long long count, float *out)
 {
-    for (long long e = 0; e < M; e++) {
+    for (long long e = 0; e < count; e++) {
         double c, s;
         exact_root(e, M, &c, &s);
         const double re = c, im = -s;
@@ -440,13 +506,19 @@ int grid_for(const void *fn, bool bf16, long long ntiles)
         if (!done.count({dev, fn})) {
             check_cuda(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes(bf16)),
                        "tensor-core kernel shared memory opt-in");
+            check_cuda(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                            cudaSharedmemCarveoutMaxShared),
+                       "tensor-core kernel carveout");
             done.insert({dev, fn});
         }
     }
     int per_sm = 0, sms = 0;
     check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, THREADS, smem_bytes(bf16)), "occupancy");
     check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
-    return (int)std::max<long long>(1, std::min<long long>(ntiles, (long long)std::max(1, per_sm) * sms));
+    // CTAs only loop over independent tiles, so a grid above what is
+    // resident is safe; never plan for fewer than the static residency
+    per_sm = std::max(per_sm, bf16 ? Smem<true>::MIN_BLOCKS : Smem<false>::MIN_BLOCKS);
+    return (int)std::max<long long>(1, std::min<long long>(ntiles, (long long)per_sm * sms));
 }
 
 }  // namespace tcf
@@ -465,11 +537,11 @@ void TCCore::init(int mode_, int logn_, long long batch_hint)
     for (int inv = 0; inv < 2; inv++)
         bmat[inv] = cached_table("tc/bmat/" + std::to_string(bf16) + "/" + std::to_string(inv), GFFT_F32, bcount,
                                  [bf16, inv](void *buf) { tcf::fill_bmat(bf16, inv != 0, (unsigned char *)buf); });
-    tw256 = cached_table("tc/w256", GFFT_F32, 512, [](void *buf) { tcf::fill_pairs(256, (float *)buf); });
+    tw256 = cached_table("tc/w256", GFFT_F32, 512, [](void *buf) { tcf::fill_pairs(256, 256, (float *)buf); });
     if (logn == 12)
-        tw4096 = cached_table("tc/w4096", GFFT_F32, 8192, [](void *buf) { tcf::fill_pairs(4096, (float *)buf); });
+        tw2 = cached_table("tc/w4096lo", GFFT_F32, 32, [](void *buf) { tcf::fill_pairs(4096, 16, (float *)buf); });
     if (logn == 16) {
-        twN = cached_table("tc/w65536", GFFT_F32, 131072, [](void *buf) { tcf::fill_pairs(65536, (float *)buf); });
+        tw2 = cached_table("tc/w65536lo", GFFT_F32, 512, [](void *buf) { tcf::fill_pairs(65536, 256, (float *)buf); });
         group = std::max<long long>(1, std::min<long long>(std::max<long long>(1, batch_hint), 1024));
         ws_bytes = (size_t)group * 65536 * 8;
         check_cuda(cudaMalloc(&ws, ws_bytes), "cudaMalloc(workspace)");
@@ -496,6 +568,13 @@ void TCCore::run(int inverse, const void *in, void *out, long long batch, long l
     const bool bf16 = mode == GFFT_MODE_TC_BF16;
     auto launch = [&](int kind, const void *src, void *dst, long long ntiles, long long nb, long long id,
                       long long od) {
+        // TMA copies need 16-byte aligned tiles: aligned base, even distance
+        CUtensorMap map;
+        std::memset(&map, 0, sizeof map);
+        bool tma = ((uintptr_t)src % 16 == 0) && (id % 2 == 0);
+        if (tma && kind == tcf::KCOL)
+            tma = make_tensor_map_3d(&map, src, 256, 256, (unsigned long long)nb, 256 * 8,
+                                     (unsigned long long)((nb > 1 ? id : 65536) * 8), 16, 256);
         tcf::TcArgs a;
         a.in = static_cast<const float2 *>(src);
         a.out = static_cast<float2 *>(dst);
@@ -505,12 +584,12 @@ void TCCore::run(int inverse, const void *in, void *out, long long batch, long l
         a.odist = od;
         a.bmat = bmat[inverse ? 1 : 0];
         a.tw256 = static_cast<const float2 *>(tw256);
-        a.tw4096 = static_cast<const float2 *>(tw4096);
-        a.twN = static_cast<const float2 *>(twN);
+        a.tw2 = static_cast<const float2 *>(tw2);
         a.err = device_error_word();
+        a.tma = tma ? 1 : 0;
         const void *fn = tcf::kernel_for(bf16, kind, inverse != 0);
         const int grid = tcf::grid_for(fn, bf16, ntiles);
-        void *args[] = {&a};
+        void *args[] = {&map, &a};
         check_cuda(cudaLaunchKernel(fn, dim3(grid), dim3(tcf::THREADS), args, tcf::smem_bytes(bf16), st),
                    "launch tensor-core C2C");
     };
