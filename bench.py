@@ -502,7 +502,7 @@ def run_ragged(args):
                        "parallelism": f"replicas x{world}"},
             "uniform_size_classes": {"gbs": round(uni_gbs, 2), "ms_per_exec": round(uni_ms, 4),
                                      "ragged_over_uniform_time_per_byte": round(exec_ms / uni_ms, 3)},
-            "autotune": {"passes_per_item": tune[0], "ctas_per_sm": tune[1], "large_first": tune[2]},
+            "autotune": {"lag_factor": tune[0], "ctas_per_sm": tune[1], "large_first": tune[2]},
             "roofline": {"bound": "hbm", "achieved": round(bytes_exec / (exec_ms / 1e3) / 1e9, 1), "peak": peak,
                          "unit": "GB/s", "frac": round(bytes_exec / (exec_ms / 1e3) / 1e9 / peak, 4),
                          "traffic": traffic_from_profile(args.workload), "peak_source": peak_src,

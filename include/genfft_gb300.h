@@ -204,9 +204,10 @@ gfft_status gfft_ragged_exec(gfft_ragged plan, int inverse, void *out, const voi
 /* adjoint of direction `inverse` (the conjugate-direction transform) */
 gfft_status gfft_ragged_exec_adjoint(gfft_ragged plan, int inverse, void *out, const void *in, void *stream);
 /* Times the candidate schedules on these buffers and keeps the fastest;
- * params = {transform passes per work item, CTAs per SM (0 = occupancy),
- * large transforms first}; *ms = its time.  With GFFT_AUTOTUNE_CACHE set
- * the choice is cached in that file per size histogram. */
+ * params = {row-tile lag (in multiples of the work items in flight), CTAs
+ * per SM (0 = occupancy), large transforms first}; *ms = its time.  With
+ * GFFT_AUTOTUNE_CACHE set the choice is cached in that file per size
+ * histogram. */
 gfft_status gfft_ragged_autotune(gfft_ragged plan, void *out, const void *in, void *stream, int *params,
                                  double *ms);
 /* total complex elements of the packed batch */
