@@ -78,13 +78,14 @@ void C2CCore::init(int dtype_, int logn_, long long batch_hint)
 
     int nvar = 0;
     const FourStepKernel *const *vars = fourstep_variants(dtype, logn, &nvar);
-    // the persistent kernel is the faster one for fp32 up to 2^18 points
-    // (measured); above that, and for fp64, the tile launches are
-    const bool fs_default = dtype == GFFT_F32 && logn <= 18;
+    // measured on GB300 (batches of 770 transforms of 2^15 .. 2^18 points,
+    // 385 of 2^19, ...): the persistent kernel is the faster one for fp32
+    // n = 2^16 .. 2^19; the tile launches for 2^15, for 2^20 and above, and
+    // for fp64
+    const bool fs_default = dtype == GFFT_F32 && logn >= 16 && logn <= 19;
     if (nvar > 0 && env_ll("GFFT_FS", fs_default ? 1 : 0) != 0) {
-        // persistent four-step: the widest tile of 64-byte runs or more
-        // that keeps three CTAs per SM, else the widest tile (or the tile
-        // width / stage count GFFT_FS_CC / GFFT_FS_NS name)
+        // persistent four-step (the tile width / stage count GFFT_FS_CC /
+        // GFFT_FS_NS name, else the rule below)
         fs = vars[0];
         const long long want_cc = env_ll("GFFT_FS_CC", 0), want_ns = env_ll("GFFT_FS_NS", 0);
         if (want_cc || want_ns) {
@@ -94,9 +95,10 @@ void C2CCore::init(int dtype_, int logn_, long long batch_hint)
                     break;
                 }
         } else {
+            // 256 compute threads (two or three CTAs per SM) with column
+            // runs of 64 bytes or more, else the widest tile
             for (int i = 0; i < nvar; i++)
-                if (vars[i]->smem <= 75 * 1024 && vars[i]->cc * (int)cplx_bytes(dtype) >= 64 &&
-                    vars[i]->cr * (int)cplx_bytes(dtype) >= 64) {
+                if (vars[i]->threads == 256 + 32 && vars[i]->cc * (int)cplx_bytes(dtype) >= 64) {
                     fs = vars[i];
                     break;
                 }
