@@ -52,10 +52,16 @@ WORKLOADS = {
 MODE_NAMES = {0: "plain", 1: "tc_fp16", 2: "tc_bf16"}
 
 
+BATCH_OVERRIDE = None  # --batch: a smaller batch of the same workload (profiling captures)
+
+
 def workload(name):
     """(kind, dtype, n0, n1, batch, mode)"""
     w = WORKLOADS[name]
-    return w if len(w) == 6 else w + (0,)
+    w = w if len(w) == 6 else w + (0,)
+    if BATCH_OVERRIDE:
+        w = w[:4] + (BATCH_OVERRIDE,) + w[5:]
+    return w
 DEFAULT = "c2c_f32_4096x16384"
 
 THROTTLE_BITS = {
@@ -406,7 +412,7 @@ def run_ragged(args):
     world, rank, local = dist_setup()
     dev = local if world > 1 else 0
     torch.cuda.set_device(dev)
-    sizes = ragged_sizes(WORKLOADS[args.workload][4])
+    sizes = ragged_sizes(workload(args.workload)[4])
     plan = G.RaggedPlan(sizes)
     gen = torch.Generator(device="cuda").manual_seed(7 + rank)
     x = torch.randn(plan.elements, dtype=torch.complex64, device="cuda", generator=gen)
@@ -694,7 +700,11 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT)
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--cpu-budget", type=float, default=8.0)
+    ap.add_argument("--batch", type=int, default=0,
+                    help="override the workload's batch (ragged: transform count); for small profiling captures")
     args = ap.parse_args()
+    global BATCH_OVERRIDE
+    BATCH_OVERRIDE = args.batch or None
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)
