@@ -56,6 +56,7 @@ SIGNATURES = {
     "gfft_exec": [_P, _I, _P, _P, _P],
     "gfft_exec_host": [_P, _I, _P, _P],
     "gfft_exec_adjoint": [_P, _I, _P, _P, _P],
+    "gfft_exec_scaled": [_P, _I, ctypes.c_double, _P, _P, _P],
     "gfft_plan_launches": [_P, ctypes.POINTER(_I)],
     "gfft_plan_workspace_size": [_P, ctypes.POINTER(ctypes.c_size_t)],
     "gfft_fft_transform": [_I, _I, _LL, _I, _P, _P, _P],
@@ -145,9 +146,14 @@ class Plan:
     def exec_ptr(self, out_ptr: int, in_ptr: int, inverse: bool = False, stream_ptr: int = 0):
         _check(lib().gfft_exec(self._h, int(inverse), out_ptr, in_ptr, stream_ptr))
 
-    def exec(self, out, x, inverse: bool = False, stream=None):
-        """Run on torch CUDA tensors (current stream)."""
-        self.exec_ptr(out.data_ptr(), x.data_ptr(), inverse, _stream_ptr(stream))
+    def exec(self, out, x, inverse: bool = False, stream=None, scale: float = 1.0):
+        """Run on torch CUDA tensors (current stream); `scale` multiplies every
+        output inside the kernel that writes it."""
+        if scale == 1.0:
+            self.exec_ptr(out.data_ptr(), x.data_ptr(), inverse, _stream_ptr(stream))
+        else:
+            _check(lib().gfft_exec_scaled(self._h, int(inverse), float(scale), out.data_ptr(), x.data_ptr(),
+                                          _stream_ptr(stream)))
         return out
 
     def adjoint_ptr(self, out_ptr: int, in_ptr: int, inverse: bool = False, stream_ptr: int = 0):

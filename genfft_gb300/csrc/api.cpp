@@ -252,7 +252,10 @@ static bool overlaps(const void *a, size_t an, const void *b, size_t bn)
     return x < y + bn && y < x + an;
 }
 
-static void exec_plan(gfft_plan_s &p, int inverse, void *out, const void *in, const Layout &L, cudaStream_t st)
+// `scale` multiplies every output (norm= scaling), applied by the kernel
+// that writes the result
+static void exec_plan(gfft_plan_s &p, int inverse, void *out, const void *in, const Layout &L, cudaStream_t st,
+                      double scale = 1.0)
 {
     const gfft_desc &d = p.d;
     const size_t cb = cplx_bytes(d.dtype), rb = real_bytes(d.dtype);
@@ -271,11 +274,11 @@ static void exec_plan(gfft_plan_s &p, int inverse, void *out, const void *in, co
                 check_cuda(cudaMemcpyAsync(out, in, (size_t)(L.batch * L.idist) * cb, cudaMemcpyDeviceToDevice, st),
                            "copy");
             check_cuda(launch_bitrev_swap(d.dtype, out, p.c2c.logn, L.batch, L.odist, st), "bit reversal");
-            p.c2c.run(inverse, out, out, L.batch, L.odist, L.odist, 1, 1, st);
+            p.c2c.run(inverse, out, out, L.batch, L.odist, L.odist, 1, 1, st, scale);
         } else if (d.mode != GFFT_MODE_PLAIN) {
-            p.tc.run(inverse, in, out, L.batch, L.idist, L.odist, L.istride, L.ostride, st);
+            p.tc.run(inverse, in, out, L.batch, L.idist, L.odist, L.istride, L.ostride, st, scale);
         } else {
-            p.c2c.run(inverse, in, out, L.batch, L.idist, L.odist, L.istride, L.ostride, st);
+            p.c2c.run(inverse, in, out, L.batch, L.idist, L.odist, L.istride, L.ostride, st, scale);
         }
         break;
     case GFFT_KIND_R2C: {
@@ -284,12 +287,12 @@ static void exec_plan(gfft_plan_s &p, int inverse, void *out, const void *in, co
             // (bins), its input layout the output (reals); unscaled
             if (overlaps(in, (size_t)(L.batch * L.odist) * cb, out, (size_t)(L.batch * L.idist) * rb))
                 fail(GFFT_ERR_ALIAS, "half-spectrum inverse: output must not overlap the input");
-            p.c2r.run(in, out, L.batch, L.odist, L.idist, 0, st);
+            p.c2r.run(in, out, L.batch, L.odist, L.idist, 0, st, scale);
             break;
         }
         if (overlaps(in, (size_t)(L.batch * L.idist) * rb, out, (size_t)(L.batch * L.odist) * cb))
             fail(GFFT_ERR_ALIAS, "real-input transform: output must not overlap the input");
-        p.r2c.run(in, out, L.batch, L.idist, L.odist, st);
+        p.r2c.run(in, out, L.batch, L.idist, L.odist, st, -1, scale);
         break;
     }
     case GFFT_KIND_C2C_2D: {
@@ -303,7 +306,7 @@ static void exec_plan(gfft_plan_s &p, int inverse, void *out, const void *in, co
                           static_cast<char *>(out) + (size_t)(b * L.odist) * cb, H, L.istride, L.ostride, 1, 1, st);
         }
         // column FFTs in place (FFTVert::transform_no_scramble, fft.h:217)
-        p.col.run(inverse, out, out, W, L.ostride, L.ostride, L.batch, L.odist, L.odist, st);
+        p.col.run(inverse, out, out, W, L.ostride, L.ostride, L.batch, L.odist, L.odist, st, scale);
         break;
     }
     case GFFT_KIND_R2C_2D: {
@@ -320,14 +323,14 @@ static void exec_plan(gfft_plan_s &p, int inverse, void *out, const void *in, co
         }
         // columns 0 .. W/2 (the non-redundant half), plus the Hermitian
         // mirror of columns 1 .. W/2-1 for the full-width layout
-        p.col.run(0, out, out, W / 2 + 1, L.ostride, L.ostride, L.batch, L.odist, L.odist, st);
+        p.col.run(0, out, out, W / 2 + 1, L.ostride, L.ostride, L.batch, L.odist, L.odist, st, scale);
         break;
     }
     case GFFT_KIND_VERT: {
         const long long cols = d.n1;
         if (out != in && overlaps(in, (size_t)(L.batch * L.idist) * cb, out, (size_t)(L.batch * L.odist) * cb))
             fail(GFFT_ERR_ALIAS, "column transform: output must be the input or not overlap it");
-        p.col.run(inverse, in, out, cols, L.istride, L.ostride, L.batch, L.idist, L.odist, st);
+        p.col.run(inverse, in, out, cols, L.istride, L.ostride, L.batch, L.idist, L.odist, st, scale);
         break;
     }
     default:
@@ -540,6 +543,14 @@ gfft_status gfft_exec(gfft_plan plan, int inverse, void *out, const void *in, vo
     GFFT_GUARD({
         gfft_plan_s *p = checked(plan);
         exec_plan(*p, inverse != 0, out, in, plan_layout(*p), (cudaStream_t)stream);
+    });
+}
+
+gfft_status gfft_exec_scaled(gfft_plan plan, int inverse, double scale, void *out, const void *in, void *stream)
+{
+    GFFT_GUARD({
+        gfft_plan_s *p = checked(plan);
+        exec_plan(*p, inverse != 0, out, in, plan_layout(*p), (cudaStream_t)stream, scale);
     });
 }
 

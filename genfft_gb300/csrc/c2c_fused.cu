@@ -42,7 +42,7 @@ template <typename T, int LOGN, bool INV>
 __global__ void __launch_bounds__(FusedCfg<T, LOGN>::THREADS)
     k_c2c_fused(const cpx<T> *__restrict__ in, cpx<T> *__restrict__ out, long long batch,
                 long long idist, long long odist, long long istride, long long ostride,
-                const cpx<T> *__restrict__ tw)
+                const cpx<T> *__restrict__ tw, T scale)
 {
     using Cfg = FusedCfg<T, LOGN>;
     using SP = typename Cfg::SP;
@@ -70,7 +70,7 @@ __global__ void __launch_bounds__(FusedCfg<T, LOGN>::THREADS)
     if (active) {
         cpx<T> *dst = out + b * odist + (long long)t * ostride;
 #pragma unroll
-        for (int q = 0; q < E; q++) stcs_c(dst + (long long)q * G * ostride, v[q]);
+        for (int q = 0; q < E; q++) stcs_c(dst + (long long)q * G * ostride, scl(v[q], scale));
     }
 }
 
@@ -154,8 +154,11 @@ cudaError_t launch_fused_c2c(int dtype, int logn, int inverse, const FusedC2CArg
     long long batch = a.batch, idist = a.idist, odist = a.odist, istride = a.istride,
               ostride = a.ostride;
     const void *tw = a.tw;
-    void *args[] = {(void *)&in, (void *)&out, (void *)&batch, (void *)&idist, (void *)&odist,
-                    (void *)&istride, (void *)&ostride, (void *)&tw};
+    float scale_f = (float)a.scale;
+    double scale_d = a.scale;
+    void *args[] = {(void *)&in,      (void *)&out,     (void *)&batch, (void *)&idist, (void *)&odist,
+                    (void *)&istride, (void *)&ostride, (void *)&tw,
+                    dtype == GFFT_F32 ? (void *)&scale_f : (void *)&scale_d};
     return cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(e.threads), args, e.smem, st);
 }
 

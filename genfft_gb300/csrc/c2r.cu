@@ -80,7 +80,7 @@ struct C2RCfg {
 template <typename T, int LOGH, int W>
 __global__ void __launch_bounds__(C2RCfg<T, LOGH>::THREADS)
     k_c2r_fused(const cpx<T> *__restrict__ in, T *__restrict__ out, long long batch, long long idist,
-                long long odist, const cpx<T> *__restrict__ tw, const cpx<T> *__restrict__ dtw)
+                long long odist, const cpx<T> *__restrict__ tw, const cpx<T> *__restrict__ dtw, T scale)
 {
     using Cfg = C2RCfg<T, LOGH>;
     using SP = typename Cfg::SP;
@@ -113,7 +113,7 @@ __global__ void __launch_bounds__(C2RCfg<T, LOGH>::THREADS)
     if (active) {
         cpx<T> *dst = reinterpret_cast<cpx<T> *>(out + b * odist) + t;
 #pragma unroll
-        for (int q = 0; q < E; q++) stcs_c(dst + q * G, v[q]);
+        for (int q = 0; q < E; q++) stcs_c(dst + q * G, scl(v[q], scale));
     }
 }
 
@@ -140,11 +140,11 @@ __global__ void k_c2r_pre(const cpx<T> *in, cpx<T> *out, long long H, long long 
 
 // n == 1: x_0 = Re F_0
 template <typename T>
-__global__ void k_c2r_one(const cpx<T> *in, T *out, long long batch, long long idist, long long odist)
+__global__ void k_c2r_one(const cpx<T> *in, T *out, long long batch, long long idist, long long odist, T scale)
 {
     for (long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x; b < batch;
          b += (long long)gridDim.x * blockDim.x)
-        out[b * odist] = ld_c(in + b * idist).x;
+        out[b * odist] = ld_c(in + b * idist).x * scale;
 }
 
 // ---------------------------------------------------------------------------
@@ -220,15 +220,17 @@ void pre_launch(int w, unsigned g, const void *in, void *out, long long H, long 
 int c2r_fused_max_logh(int dtype) { return dtype == GFFT_F32 ? C2RMax<float>::value : C2RMax<double>::value; }
 
 cudaError_t launch_c2r_fused(int dtype, int logh, int wmode, const void *in, void *out, long long batch,
-                             long long idist, long long odist, const void *tw, const void *dtw, cudaStream_t st)
+                             long long idist, long long odist, const void *tw, const void *dtw, cudaStream_t st,
+                             double scale)
 {
     const C2REntry &e = c2r_entry(dtype, logh);
     const void *fn = e.fn[wmode];
     cudaError_t err = smem_optin2(fn, e.smem);
     if (err != cudaSuccess) return err;
     const long long grid = (batch + e.tpc - 1) / e.tpc;
-    void *args[] = {(void *)&in, (void *)&out, (void *)&batch, (void *)&idist, (void *)&odist, (void *)&tw,
-                    (void *)&dtw};
+    float scale_f = (float)scale;
+    void *args[] = {(void *)&in,  (void *)&out, (void *)&batch, (void *)&idist, (void *)&odist, (void *)&tw,
+                    (void *)&dtw, dtype == GFFT_F32 ? (void *)&scale_f : (void *)&scale};
     return cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(e.threads), args, e.smem, st);
 }
 
@@ -242,11 +244,12 @@ cudaError_t launch_c2r_pre(int dtype, int wmode, const void *in, void *out, long
 }
 
 cudaError_t launch_c2r_one(int dtype, const void *in, void *out, long long batch, long long idist, long long odist,
-                           cudaStream_t st)
+                           cudaStream_t st, double scale)
 {
     const unsigned g = grid_for2(batch, 256);
-    if (dtype == GFFT_F32) k_c2r_one<float><<<g, 256, 0, st>>>((const cpx<float> *)in, (float *)out, batch, idist, odist);
-    else k_c2r_one<double><<<g, 256, 0, st>>>((const cpx<double> *)in, (double *)out, batch, idist, odist);
+    if (dtype == GFFT_F32)
+        k_c2r_one<float><<<g, 256, 0, st>>>((const cpx<float> *)in, (float *)out, batch, idist, odist, (float)scale);
+    else k_c2r_one<double><<<g, 256, 0, st>>>((const cpx<double> *)in, (double *)out, batch, idist, odist, scale);
     return cudaGetLastError();
 }
 

@@ -49,6 +49,9 @@ __device__ __forceinline__ cpx<T> twmul(cpx<T> a, cpx<T> w)
 }
 template <typename T>
 __device__ __forceinline__ cpx<T> conj(cpx<T> a) { return {a.x, -a.y}; }
+// a * s for a real scale (the norm= factor of a transform's last store)
+template <typename T>
+__device__ __forceinline__ cpx<T> scl(cpx<T> a, T s) { return {a.x * s, a.y * s}; }
 
 __host__ __device__ constexpr int ipow(int b, int e) { return e <= 0 ? 1 : b * ipow(b, e - 1); }
 

@@ -335,12 +335,13 @@ __global__ void __launch_bounds__(FourStepCfg<T, LA, LB, CC, E_, NS_>::THREADS,
             for (int q = 0; q < EB; q++) S[spad<T>((tt + q * GB) * CR + s)] = v[q];
             bar_compute(CT);
             cpx<T> *dst = static_cast<cpx<T> *>(a.out) + t * a.odist + row0;
+            const T scale = (T)a.scale;
 #pragma unroll
             for (int m = 0; m < EB; m++) {
                 const int idx = tid + m * CT;
                 const int s2 = idx % CR;
                 const int kk = idx / CR;
-                stcs_c(dst + s2 + (long long)kk * A, S[spad<T>(idx)]);
+                stcs_c(dst + s2 + (long long)kk * A, scl(S[spad<T>(idx)], scale));
             }
             bar_compute(CT);
             if (tid == 0) mbar_arrive(&empty[st]);

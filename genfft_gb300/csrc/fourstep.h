@@ -22,6 +22,7 @@ struct FourStepArgs {
     int lo_bits;
     int slots, lag;
     int nitems;
+    double scale;             // applied to every output (norm= scaling)
 };
 
 struct FourStepKernel {

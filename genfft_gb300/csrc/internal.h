@@ -29,6 +29,7 @@ struct FusedC2CArgs {
     long long idist, odist;       // elements between transforms
     long long istride, ostride;   // elements between points
     const void *tw;               // device twiddle table for (dtype, logn)
+    double scale = 1.0;           // applied to every output (norm= scaling)
 };
 int fused_max_logn(int dtype);
 size_t fused_twiddle_count(int dtype, int logn);              // complex elements

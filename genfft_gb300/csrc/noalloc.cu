@@ -174,13 +174,15 @@ extern "C" gfft_status gfft_fft_transform_noalloc(int dtype, int n, long long ba
             long long ncols = B, ld_in = B, ld_out = B, idist = N, odist = N;
             int lob = lo;
             unsigned nm = nmask;
-            void *cargs[] = {&src, &ws, &ncols, &ld_in, &ld_out, &idist, &odist, &tw_col, &tw_lo, &tw_hi, &lob, &nm};
+            float one = 1.0f;
+            void *cargs[] = {&src, &ws, &ncols, &ld_in, &ld_out, &idist, &odist, &tw_col, &tw_lo, &tw_hi, &lob, &nm,
+                             &one};
             check_cuda(cudaLaunchKernel(fc, dim3((unsigned)(B / s.ccol[logn]), (unsigned)nb), dim3(kc.threads), cargs,
                                         kc.smem, st),
                        "launch column pass");
             long long nrows = A, rld = B, ostride = A, ridist = N, rodist = N;
             const cpx<float> *wsc = ws;
-            void *rargs[] = {&wsc, &dst, &nrows, &rld, &ostride, &ridist, &rodist, &tw_row};
+            void *rargs[] = {&wsc, &dst, &nrows, &rld, &ostride, &ridist, &rodist, &tw_row, &one};
             check_cuda(cudaLaunchKernel(fr, dim3((unsigned)(A / s.crow[logn]), (unsigned)nb), dim3(kr.threads), rargs,
                                         kr.smem, st),
                        "launch row pass");

@@ -151,10 +151,10 @@ int C2CCore::launches(long long batch) const
 }
 
 void C2CCore::run(int inverse, const void *in, void *out, long long batch, long long idist, long long odist,
-                  long long istride, long long ostride, cudaStream_t st) const
+                  long long istride, long long ostride, cudaStream_t st, double scale) const
 {
     if (algo == 1) {
-        FusedC2CArgs a{in, out, batch, idist, odist, istride, ostride, tw};
+        FusedC2CArgs a{in, out, batch, idist, odist, istride, ostride, tw, scale};
         check_cuda(launch_fused_c2c(dtype, logn, inverse, a, st), "launch fused C2C");
         return;
     }
@@ -194,6 +194,7 @@ void C2CCore::run(int inverse, const void *in, void *out, long long batch, long 
             a.slots = fs_slots;
             a.lag = fs_lag;
             a.nitems = (int)((nb + fs_lag) * (fs->nc + fs->nr));
+            a.scale = scale;
             check_cuda(launch_fourstep(*fs, inverse, map, a, fs_grid, st), "launch persistent four-step");
             launched = true;
         }
@@ -211,7 +212,7 @@ void C2CCore::run(int inverse, const void *in, void *out, long long batch, long 
                                   lo_bits, nmask, st),
                    "launch column pass");
         // row pass: A rows of B points, stored transposed (stride A)
-        check_cuda(launch_rowpass(*krow, inverse, A / crow, nb, ws, dst, A, B, A, N, odist, tw_row, st),
+        check_cuda(launch_rowpass(*krow, inverse, A / crow, nb, ws, dst, A, B, A, N, odist, tw_row, st, scale),
                    "launch row pass");
     }
 }
@@ -232,10 +233,10 @@ void ColCore::init(int dtype_, int logl_, int variant_)
 }
 
 void ColCore::run(int inverse, const void *in, void *out, long long ncols, long long ld_in, long long ld_out,
-                  long long batch, long long idist, long long odist, cudaStream_t st) const
+                  long long batch, long long idist, long long odist, cudaStream_t st, double scale) const
 {
     check_cuda(launch_colpass(*k, inverse, (ncols + c - 1) / c, batch, in, out, ncols, ld_in, ld_out, idist, odist,
-                              tw, nullptr, nullptr, 0, 0u, st),
+                              tw, nullptr, nullptr, 0, 0u, st, scale),
                "launch column FFT");
 }
 
@@ -271,20 +272,20 @@ int R2CCore::launches(long long batch) const
 }
 
 void R2CCore::run(const void *in, void *out, long long batch, long long idist, long long odist, cudaStream_t st,
-                  int mode) const
+                  int mode, double scale) const
 {
     if (mode < 0) mode = half ? 0 : 1;
     if (algo == 0) {
-        check_cuda(launch_r2c_one(dtype, in, out, batch, idist, odist, st), "launch R2C n=1");
+        check_cuda(launch_r2c_one(dtype, in, out, batch, idist, odist, st, scale), "launch R2C n=1");
     } else if (algo == 1) {
-        check_cuda(launch_r2c_fused(dtype, logn - 1, mode, in, out, batch, idist, odist, tw, dtw, st),
+        check_cuda(launch_r2c_fused(dtype, logn - 1, mode, in, out, batch, idist, odist, tw, dtw, st, scale),
                    "launch fused R2C");
     } else {
         const long long H = 1LL << (logn - 1);
         // n reals are n/2 complex; transform them into the output buffer,
         // then adjust in place (the reference's order, FFTReal.h:209-211)
         c2c.run(0, in, out, batch, idist / 2, odist, 1, 1, st);
-        check_cuda(launch_dit(dtype, mode, out, out, H, batch, odist, odist, dtw, st), "launch DIT pass");
+        check_cuda(launch_dit(dtype, mode, out, out, H, batch, odist, odist, dtw, st, scale), "launch DIT pass");
     }
 }
 
@@ -321,19 +322,19 @@ int C2RCore::launches(long long batch) const
 }
 
 void C2RCore::run(const void *in, void *out, long long batch, long long idist, long long odist, int wmode,
-                  cudaStream_t st) const
+                  cudaStream_t st, double scale) const
 {
     if (algo == 0) {
-        check_cuda(launch_c2r_one(dtype, in, out, batch, idist, odist, st), "launch C2R n=1");
+        check_cuda(launch_c2r_one(dtype, in, out, batch, idist, odist, st, scale), "launch C2R n=1");
     } else if (algo == 1) {
-        check_cuda(launch_c2r_fused(dtype, logn - 1, wmode, in, out, batch, idist, odist, tw, dtw, st),
+        check_cuda(launch_c2r_fused(dtype, logn - 1, wmode, in, out, batch, idist, odist, tw, dtw, st, scale),
                    "launch fused C2R");
     } else {
         const long long H = 1LL << (logn - 1);
         // Z' (n/2 complex = the n output reals) into the output buffer, then
         // the unscaled inverse C2C of n/2 points in place
         check_cuda(launch_c2r_pre(dtype, wmode, in, out, H, batch, idist, odist / 2, dtw, st), "launch C2R pre-pass");
-        c2c.run(1, out, out, batch, odist / 2, odist / 2, 1, 1, st);
+        c2c.run(1, out, out, batch, odist / 2, odist / 2, 1, 1, st, scale);
     }
 }
 

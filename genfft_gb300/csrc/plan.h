@@ -39,7 +39,7 @@ struct C2CCore {
     int launches(long long batch) const;
     // strides in complex elements; four-step needs unit element strides
     void run(int inverse, const void *in, void *out, long long batch, long long idist, long long odist,
-             long long istride, long long ostride, cudaStream_t st) const;
+             long long istride, long long ostride, cudaStream_t st, double scale = 1.0) const;
 };
 
 // Column FFTs of length 2^logl over ncols columns (tile kernels).
@@ -49,7 +49,7 @@ struct ColCore {
     const void *tw = nullptr;
     void init(int dtype, int logl, int variant);
     void run(int inverse, const void *in, void *out, long long ncols, long long ld_in, long long ld_out,
-             long long batch, long long idist, long long odist, cudaStream_t st) const;
+             long long batch, long long idist, long long odist, cudaStream_t st, double scale = 1.0) const;
 };
 
 // Real-input 1D transform of n = 2^logn reals (RealFFT<T>::forward).
@@ -64,7 +64,7 @@ struct R2CCore {
     int launches(long long batch) const;
     // idist in reals (even), odist in complex elements
     void run(const void *in, void *out, long long batch, long long idist, long long odist, cudaStream_t st,
-             int mode = -1) const;
+             int mode = -1, double scale = 1.0) const;
 };
 
 // Half-spectrum inverse: n/2+1 bins -> n reals, unscaled, Hermitian
@@ -79,7 +79,7 @@ struct C2RCore {
     int launches(long long batch) const;
     // idist in complex elements, odist in reals (even)
     void run(const void *in, void *out, long long batch, long long idist, long long odist, int wmode,
-             cudaStream_t st) const;
+             cudaStream_t st, double scale = 1.0) const;
 };
 
 // Split-precision tensor-core C2C (tc.cu): fp32 data, radix-16 DFT blocks
@@ -95,7 +95,7 @@ struct TCCore {
     void release();
     int launches(long long batch) const;
     void run(int inverse, const void *in, void *out, long long batch, long long idist, long long odist,
-             long long istride, long long ostride, cudaStream_t st) const;
+             long long istride, long long ostride, cudaStream_t st, double scale = 1.0) const;
 };
 
 // ---- kernels in real.cu --------------------------------------------------
@@ -106,22 +106,24 @@ void dit_twiddle_fill(int dtype, int logn, void *buf);
 // mode: 0 half spectrum, 1 full spectrum, 2 half with doubled interior
 // bins (the adjoint of the half-spectrum C2R)
 cudaError_t launch_r2c_fused(int dtype, int logh, int mode, const void *in, void *out, long long batch,
-                             long long idist, long long odist, const void *tw, const void *dtw, cudaStream_t st);
+                             long long idist, long long odist, const void *tw, const void *dtw, cudaStream_t st,
+                             double scale = 1.0);
 cudaError_t launch_dit(int dtype, int mode, const void *in, void *out, long long H, long long batch,
-                       long long idist, long long odist, const void *dtw, cudaStream_t st);
+                       long long idist, long long odist, const void *dtw, cudaStream_t st, double scale = 1.0);
 // C2R (c2r.cu): weighting 0 = as given (Hermitian extension), 1 = interior
 // bins halved (adjoint of the half-spectrum R2C), 2 = n-bin input folded
 // (g_k + conj g_{n-k}) / 2 (adjoint of the full-spectrum R2C)
 int c2r_fused_max_logh(int dtype);
 cudaError_t launch_c2r_fused(int dtype, int logh, int wmode, const void *in, void *out, long long batch,
-                             long long idist, long long odist, const void *tw, const void *dtw, cudaStream_t st);
+                             long long idist, long long odist, const void *tw, const void *dtw, cudaStream_t st,
+                             double scale = 1.0);
 cudaError_t launch_c2r_pre(int dtype, int wmode, const void *in, void *out, long long H, long long batch,
                            long long idist, long long odist, const void *dtw, cudaStream_t st);
 cudaError_t launch_c2r_one(int dtype, const void *in, void *out, long long batch, long long idist, long long odist,
-                           cudaStream_t st);
+                           cudaStream_t st, double scale = 1.0);
 cudaError_t launch_dit_one(int dtype, const void *in, void *out, cudaStream_t st);
 cudaError_t launch_r2c_one(int dtype, const void *in, void *out, long long batch, long long idist, long long odist,
-                           cudaStream_t st);
+                           cudaStream_t st, double scale = 1.0);
 cudaError_t launch_separate2x(int dtype, const void *in, void *o1, void *o2, long long n, cudaStream_t st);
 cudaError_t launch_interleave(int dtype, const void *a, long long lda, const void *b, long long ldb, void *z,
                               long long ldz, long long rows, long long cols, cudaStream_t st);

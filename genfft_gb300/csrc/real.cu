@@ -71,7 +71,7 @@ __device__ __forceinline__ cpx<T> r2c_weight(cpx<T> f, long long k, long long H)
 template <typename T, int LOGH, int MODE>
 __global__ void __launch_bounds__(R2CCfg<T, LOGH>::THREADS)
     k_r2c_fused(const T *__restrict__ in, cpx<T> *__restrict__ out, long long batch, long long idist,
-                long long odist, const cpx<T> *__restrict__ tw, const cpx<T> *__restrict__ dtw)
+                long long odist, const cpx<T> *__restrict__ tw, const cpx<T> *__restrict__ dtw, T scale)
 {
     using Cfg = R2CCfg<T, LOGH>;
     using SP = typename Cfg::SP;
@@ -107,7 +107,7 @@ __global__ void __launch_bounds__(R2CCfg<T, LOGH>::THREADS)
         if (k > H) break;
         const int km = k & (H - 1);
         const int j = (H - k) & (H - 1);
-        const cpx<T> f = dit_value(my[spad<T>(km)], my[spad<T>(j)], ldg_c(dtw + k));
+        const cpx<T> f = scl(dit_value(my[spad<T>(km)], my[spad<T>(j)], ldg_c(dtw + k)), scale);
         stcs_c(dst + k, r2c_weight<MODE>(f, k, H));
         if constexpr (MODE == R2C_FULL) {
             if (k > 0 && k < H) stcs_c(dst + 2 * H - k, conj(f));
@@ -120,7 +120,7 @@ __global__ void __launch_bounds__(R2CCfg<T, LOGH>::THREADS)
 // values before writing, so out == in is safe.
 template <typename T, int MODE>
 __global__ void k_dit(const cpx<T> *in, cpx<T> *out, long long H, long long batch, long long idist,
-                      long long odist, const cpx<T> *__restrict__ dtw)
+                      long long odist, const cpx<T> *__restrict__ dtw, T scale)
 {
     const long long pairs = H / 2 + 1;
     for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < pairs * batch;
@@ -131,8 +131,8 @@ __global__ void k_dit(const cpx<T> *in, cpx<T> *out, long long H, long long batc
         cpx<T> *f = out + b * odist;
         const long long j = (H - k) & (H - 1);
         const cpx<T> zk = ld_c(z + (k & (H - 1))), zj = ld_c(z + j);
-        const cpx<T> fk = dit_value(zk, zj, ldg_c(dtw + k));
-        const cpx<T> fj = dit_value(zj, zk, ldg_c(dtw + (H - k)));
+        const cpx<T> fk = scl(dit_value(zk, zj, ldg_c(dtw + k)), scale);
+        const cpx<T> fj = scl(dit_value(zj, zk, ldg_c(dtw + (H - k))), scale);
         st_c(f + k, r2c_weight<MODE>(fk, k, H));
         if (H - k != k) st_c(f + (H - k), r2c_weight<MODE>(fj, H - k, H));
         if constexpr (MODE == R2C_FULL) {
@@ -144,11 +144,11 @@ __global__ void k_dit(const cpx<T> *in, cpx<T> *out, long long H, long long batc
 
 // n == 1: F_0 = x_0 (RealFFT::forward, FFTReal.h:205-207)
 template <typename T>
-__global__ void k_r2c_one(const T *in, cpx<T> *out, long long batch, long long idist, long long odist)
+__global__ void k_r2c_one(const T *in, cpx<T> *out, long long batch, long long idist, long long odist, T scale)
 {
     for (long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x; b < batch;
          b += (long long)gridDim.x * blockDim.x)
-        st_c(out + b * odist, cpx<T>{in[b * idist], (T)0});
+        st_c(out + b * odist, cpx<T>{in[b * idist] * scale, (T)0});
 }
 
 // separate_2x_real_FFT (FFTReal.h:34-66): X = FFT(x), Y = FFT(y) from
@@ -304,45 +304,48 @@ void dit_twiddle_fill(int dtype, int logn, void *buf)
 }
 
 cudaError_t launch_r2c_fused(int dtype, int logh, int mode, const void *in, void *out, long long batch,
-                             long long idist, long long odist, const void *tw, const void *dtw, cudaStream_t st)
+                             long long idist, long long odist, const void *tw, const void *dtw, cudaStream_t st,
+                             double scale)
 {
     const R2CEntry &e = r2c_entry(dtype, logh);
     const void *fn = e.fn[mode];
     cudaError_t err = smem_optin(fn, e.smem);
     if (err != cudaSuccess) return err;
     const long long grid = (batch + e.tpc - 1) / e.tpc;
-    void *args[] = {(void *)&in, (void *)&out, (void *)&batch, (void *)&idist, (void *)&odist, (void *)&tw,
-                    (void *)&dtw};
+    float scale_f = (float)scale;
+    void *args[] = {(void *)&in,  (void *)&out, (void *)&batch, (void *)&idist, (void *)&odist, (void *)&tw,
+                    (void *)&dtw, dtype == GFFT_F32 ? (void *)&scale_f : (void *)&scale};
     return cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(e.threads), args, e.smem, st);
 }
 
 template <typename T>
 void dit_launch(int mode, unsigned g, const void *in, void *out, long long H, long long batch, long long idist,
-                long long odist, const void *dtw, cudaStream_t st)
+                long long odist, const void *dtw, cudaStream_t st, T sc)
 {
     auto i = (const cpx<T> *)in;
     auto o = (cpx<T> *)out;
     auto d = (const cpx<T> *)dtw;
-    if (mode == R2C_HALF) k_dit<T, R2C_HALF><<<g, 256, 0, st>>>(i, o, H, batch, idist, odist, d);
-    else if (mode == R2C_FULL) k_dit<T, R2C_FULL><<<g, 256, 0, st>>>(i, o, H, batch, idist, odist, d);
-    else k_dit<T, R2C_HALF_X2><<<g, 256, 0, st>>>(i, o, H, batch, idist, odist, d);
+    if (mode == R2C_HALF) k_dit<T, R2C_HALF><<<g, 256, 0, st>>>(i, o, H, batch, idist, odist, d, sc);
+    else if (mode == R2C_FULL) k_dit<T, R2C_FULL><<<g, 256, 0, st>>>(i, o, H, batch, idist, odist, d, sc);
+    else k_dit<T, R2C_HALF_X2><<<g, 256, 0, st>>>(i, o, H, batch, idist, odist, d, sc);
 }
 
 cudaError_t launch_dit(int dtype, int mode, const void *in, void *out, long long H, long long batch,
-                       long long idist, long long odist, const void *dtw, cudaStream_t st)
+                       long long idist, long long odist, const void *dtw, cudaStream_t st, double scale)
 {
     const unsigned g = grid_for((H / 2 + 1) * batch, 256);
-    if (dtype == GFFT_F32) dit_launch<float>(mode, g, in, out, H, batch, idist, odist, dtw, st);
-    else dit_launch<double>(mode, g, in, out, H, batch, idist, odist, dtw, st);
+    if (dtype == GFFT_F32) dit_launch<float>(mode, g, in, out, H, batch, idist, odist, dtw, st, (float)scale);
+    else dit_launch<double>(mode, g, in, out, H, batch, idist, odist, dtw, st, scale);
     return cudaGetLastError();
 }
 
 cudaError_t launch_r2c_one(int dtype, const void *in, void *out, long long batch, long long idist, long long odist,
-                           cudaStream_t st)
+                           cudaStream_t st, double scale)
 {
     const unsigned g = grid_for(batch, 256);
-    if (dtype == GFFT_F32) k_r2c_one<float><<<g, 256, 0, st>>>((const float *)in, (cpx<float> *)out, batch, idist, odist);
-    else k_r2c_one<double><<<g, 256, 0, st>>>((const double *)in, (cpx<double> *)out, batch, idist, odist);
+    if (dtype == GFFT_F32)
+        k_r2c_one<float><<<g, 256, 0, st>>>((const float *)in, (cpx<float> *)out, batch, idist, odist, (float)scale);
+    else k_r2c_one<double><<<g, 256, 0, st>>>((const double *)in, (cpx<double> *)out, batch, idist, odist, scale);
     return cudaGetLastError();
 }
 

@@ -103,7 +103,8 @@ struct TcArgs {
     const float2 *tw256;   // W_256^e, (hi, lo) pairs
     const float2 *tw2;     // W_4096^e, e < 16 (K4096) or W_65536^e, e < 256 (KCOL): (hi, lo) pairs
     unsigned *err;
-    int tma;  // 1: TMA copies of the tiles (16-byte aligned), 0: thread loads
+    int tma;      // 1: TMA copies of the tiles (16-byte aligned), 0: thread loads
+    float scale;  // applied to every output of the last pass (norm= scaling)
 };
 
 __device__ __forceinline__ int xpad(int i) { return i + (i >> 4); }
@@ -375,13 +376,13 @@ __global__ void __launch_bounds__(THREADS, Smem<BF16>::MIN_BLOCKS)
                 if (KIND == K4096) {
                     float2 *dst = a.out + w * a.odist + m;
 #pragma unroll
-                    for (int k = 0; k < 16; k++) __stcs(dst + 256 * k, o[k]);
+                    for (int k = 0; k < 16; k++) __stcs(dst + 256 * k, make_float2(o[k].x * a.scale, o[k].y * a.scale));
                 } else if (KIND == K256) {
                     const long long t = w * 16 + (m >> 4);
                     if (t < a.batch) {
                         float2 *dst = a.out + t * a.odist + (m & 15);
 #pragma unroll
-                        for (int k = 0; k < 16; k++) __stcs(dst + 16 * k, o[k]);
+                        for (int k = 0; k < 16; k++) __stcs(dst + 16 * k, make_float2(o[k].x * a.scale, o[k].y * a.scale));
                     }
                 } else if (KIND == KCOL) {
                     // X[K] of column c, K = j + 16 k, times W_65536^(col K)
@@ -405,7 +406,8 @@ __global__ void __launch_bounds__(THREADS, Smem<BF16>::MIN_BLOCKS)
 #pragma unroll 4
                     for (int q = 0; q < 16; q++) {
                         const int i = tid + 256 * q;
-                        __stcs(dst + (i & 15) + (long long)(i >> 4) * 256, X[xpad(i)]);
+                        const float2 z = X[xpad(i)];
+                        __stcs(dst + (i & 15) + (long long)(i >> 4) * 256, make_float2(z.x * a.scale, z.y * a.scale));
                     }
                 }
             }
@@ -562,7 +564,7 @@ int TCCore::launches(long long batch) const
 }
 
 void TCCore::run(int inverse, const void *in, void *out, long long batch, long long idist, long long odist,
-                 long long istride, long long ostride, cudaStream_t st) const
+                 long long istride, long long ostride, cudaStream_t st, double scale) const
 {
     if (istride != 1 || ostride != 1) fail(GFFT_ERR_UNSUPPORTED, "the tensor-core path needs unit element strides");
     const bool bf16 = mode == GFFT_MODE_TC_BF16;
@@ -587,6 +589,7 @@ void TCCore::run(int inverse, const void *in, void *out, long long batch, long l
         a.tw2 = static_cast<const float2 *>(tw2);
         a.err = device_error_word();
         a.tma = tma ? 1 : 0;
+        a.scale = kind == tcf::KCOL ? 1.0f : (float)scale;
         const void *fn = tcf::kernel_for(bf16, kind, inverse != 0);
         const int grid = tcf::grid_for(fn, bf16, ntiles);
         void *args[] = {&map, &a};

@@ -55,7 +55,7 @@ __global__ void __launch_bounds__(ColCfg<T, LOGL, C, E_>::THREADS)
     k_colpass(const cpx<T> *__restrict__ in, cpx<T> *__restrict__ out, long long ncols, long long ld_in,
               long long ld_out, long long idist, long long odist,
               const cpx<T> *__restrict__ tw, const cpx<T> *__restrict__ tw_lo,
-              const cpx<T> *__restrict__ tw_hi, int lo_bits, unsigned nmask)
+              const cpx<T> *__restrict__ tw_hi, int lo_bits, unsigned nmask, T scale)
 {
     using Cfg = ColCfg<T, LOGL, C, E_>;
     using SP = typename Cfg::SP;
@@ -105,7 +105,7 @@ __global__ void __launch_bounds__(ColCfg<T, LOGL, C, E_>::THREADS)
                     // (each hoisted pair costs four live registers)
                     if ((q & 3) == 3) asm volatile("" ::: "memory");
                 }
-                st_c(dst, val);
+                st_c(dst, scl(val, scale));
             }
             if constexpr (HERM) {
                 const long long W = 2 * (ncols - 1);
@@ -114,7 +114,7 @@ __global__ void __launch_bounds__(ColCfg<T, LOGL, C, E_>::THREADS)
 #pragma unroll
                     for (int q = 0; q < E; q++) {
                         const int i = t + q * G;
-                        st_c(mir + (long long)((SP::N - i) & (SP::N - 1)) * ld_out, conj(v[q]));
+                        st_c(mir + (long long)((SP::N - i) & (SP::N - 1)) * ld_out, scl(conj(v[q]), scale));
                     }
                 }
             }
@@ -142,7 +142,7 @@ template <typename T, int LOGL, int C, int E_, bool INV>
 __global__ void __launch_bounds__(RowCfg<T, LOGL, C, E_>::THREADS)
     k_rowpass(const cpx<T> *__restrict__ in, cpx<T> *__restrict__ out, long long nrows, long long ld_in,
               long long ostride, long long idist, long long odist,
-              const cpx<T> *__restrict__ tw)
+              const cpx<T> *__restrict__ tw, T scale)
 {
     using Cfg = RowCfg<T, LOGL, C, E_>;
     using SP = typename Cfg::SP;
@@ -175,7 +175,7 @@ __global__ void __launch_bounds__(RowCfg<T, LOGL, C, E_>::THREADS)
             const int idx = threadIdx.x + m * Cfg::THREADS;
             const int s2 = idx % C;
             const int k = idx / C;
-            if (k < N && row0 + s2 < nrows) stcs_c(dst + s2 + (long long)k * ostride, sm[spad<T>(idx)]);
+            if (k < N && row0 + s2 < nrows) stcs_c(dst + s2 + (long long)k * ostride, scl(sm[spad<T>(idx)], scale));
         }
     }
 }

@@ -174,8 +174,11 @@ int tile_widest(int dtype, int variant, int logl, int max_c)
 cudaError_t launch_colpass(const TileKernel &k, int inverse, long long tiles, long long nbatch,
                            const void *in, void *out, long long ncols, long long ld_in, long long ld_out,
                            long long idist, long long odist, const void *tw, const void *tw_lo,
-                           const void *tw_hi, int lo_bits, unsigned nmask, cudaStream_t st)
+                           const void *tw_hi, int lo_bits, unsigned nmask, cudaStream_t st, double scale)
 {
+    // the kernels take the scale as their element type
+    float scale_f = (float)scale;
+    void *scale_p = k.elem_bytes == 8 ? (void *)&scale_f : (void *)&scale;
     // persistent TMA path: the tensor map needs 16-byte aligned base and
     // strides; in-place runs (out == in) are fine, each tile is loaded whole
     // before it is written back
@@ -200,7 +203,7 @@ cudaError_t launch_colpass(const TileKernel &k, int inverse, long long tiles, lo
             const long long grid = persistent_grid(fn, k.tma_threads, k.tma_smem, tiles * nbatch);
             void *args[] = {(void *)&map, (void *)&out, (void *)&ncols, (void *)&ld_out, (void *)&odist,
                             (void *)&nbatch, (void *)&tw, (void *)&tw_lo, (void *)&tw_hi, (void *)&lo_bits,
-                            (void *)&nmask, (void *)&err};
+                            (void *)&nmask, (void *)&err, scale_p};
             return cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(k.tma_threads), args, k.tma_smem, st);
         }
     }
@@ -209,7 +212,7 @@ cudaError_t launch_colpass(const TileKernel &k, int inverse, long long tiles, lo
     if (e != cudaSuccess) return e;
     void *args[] = {(void *)&in,    (void *)&out,   (void *)&ncols, (void *)&ld_in,
                     (void *)&ld_out, (void *)&idist, (void *)&odist, (void *)&tw,
-                    (void *)&tw_lo, (void *)&tw_hi, (void *)&lo_bits, (void *)&nmask};
+                    (void *)&tw_lo, (void *)&tw_hi, (void *)&lo_bits, (void *)&nmask, scale_p};
     for (long long b0 = 0; b0 < nbatch; b0 += 65535) {
         const long long nb = std::min<long long>(65535, nbatch - b0);
         const void *inp = static_cast<const char *>(in) + b0 * idist * (long long)k.elem_bytes;
@@ -224,8 +227,10 @@ cudaError_t launch_colpass(const TileKernel &k, int inverse, long long tiles, lo
 
 cudaError_t launch_rowpass(const TileKernel &k, int inverse, long long tiles, long long nbatch,
                            const void *in, void *out, long long nrows, long long ld_in, long long ostride,
-                           long long idist, long long odist, const void *tw, cudaStream_t st)
+                           long long idist, long long odist, const void *tw, cudaStream_t st, double scale)
 {
+    float scale_f = (float)scale;
+    void *scale_p = k.elem_bytes == 8 ? (void *)&scale_f : (void *)&scale;
     const size_t eb = (size_t)k.elem_bytes;
     if (k.tma_fwd && !tma_disabled() && aligned16(in) && (ld_in * eb) % 16 == 0 &&
         (nbatch == 1 || (idist * eb) % 16 == 0)) {
@@ -235,7 +240,7 @@ cudaError_t launch_rowpass(const TileKernel &k, int inverse, long long tiles, lo
         unsigned *err = device_error_word();
         const long long grid = persistent_grid(fn, k.tma_threads, k.tma_smem, tiles * nbatch);
         void *args[] = {(void *)&in,    (void *)&out,   (void *)&nrows, (void *)&ld_in, (void *)&ostride,
-                        (void *)&idist, (void *)&odist, (void *)&nbatch, (void *)&tw, (void *)&err};
+                        (void *)&idist, (void *)&odist, (void *)&nbatch, (void *)&tw, (void *)&err, scale_p};
         return cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(k.tma_threads), args, k.tma_smem, st);
     }
     const void *fn = inverse ? k.inv : k.fwd;
@@ -246,7 +251,7 @@ cudaError_t launch_rowpass(const TileKernel &k, int inverse, long long tiles, lo
         const void *inp = static_cast<const char *>(in) + b0 * idist * (long long)k.elem_bytes;
         void *outp = static_cast<char *>(out) + b0 * odist * (long long)k.elem_bytes;
         void *args[] = {(void *)&inp,   (void *)&outp,  (void *)&nrows, (void *)&ld_in,
-                        (void *)&ostride, (void *)&idist, (void *)&odist, (void *)&tw};
+                        (void *)&ostride, (void *)&idist, (void *)&odist, (void *)&tw, scale_p};
         e = cudaLaunchKernel(fn, dim3((unsigned)tiles, (unsigned)nb), dim3(k.threads), args, k.smem, st);
         if (e != cudaSuccess) return e;
     }

@@ -46,10 +46,10 @@ int tile_widest(int dtype, int variant, int logl, int max_c);
 cudaError_t launch_colpass(const TileKernel &k, int inverse, long long tiles, long long nbatch,
                            const void *in, void *out, long long ncols, long long ld_in, long long ld_out,
                            long long idist, long long odist, const void *tw, const void *tw_lo,
-                           const void *tw_hi, int lo_bits, unsigned nmask, cudaStream_t st);
+                           const void *tw_hi, int lo_bits, unsigned nmask, cudaStream_t st, double scale = 1.0);
 cudaError_t launch_rowpass(const TileKernel &k, int inverse, long long tiles, long long nbatch,
                            const void *in, void *out, long long nrows, long long ld_in, long long ostride,
-                           long long idist, long long odist, const void *tw, cudaStream_t st);
+                           long long idist, long long odist, const void *tw, cudaStream_t st, double scale = 1.0);
 
 // 3D tiled tensor map over 8-byte units (dims x, y, z; byte strides of y
 // and z; box bx x by x 1); false if the driver entry point is missing or

@@ -49,7 +49,7 @@ template <typename T, int LOGL, int C, int E_, bool INV>
 __global__ void __launch_bounds__(RowTmaCfg<T, LOGL, C, E_>::THREADS, 1)
     k_rowpass_tma(const cpx<T> *__restrict__ in, cpx<T> *__restrict__ out, long long nrows, long long ld_in,
                   long long ostride, long long idist, long long odist, long long nbatch,
-                  const cpx<T> *__restrict__ tw, unsigned *err)
+                  const cpx<T> *__restrict__ tw, unsigned *err, T scale)
 {
     using Cfg = RowTmaCfg<T, LOGL, C, E_>;
     using SP = typename Cfg::SP;
@@ -117,7 +117,7 @@ __global__ void __launch_bounds__(RowTmaCfg<T, LOGL, C, E_>::THREADS, 1)
             const int idx = threadIdx.x + m * Cfg::THREADS;
             const int s2 = idx % C;
             const int kk = idx / C;
-            if (kk < N && row0 + s2 < nrows) stcs_c(dst + s2 + (long long)kk * ostride, S[spad<T>(idx)]);
+            if (kk < N && row0 + s2 < nrows) stcs_c(dst + s2 + (long long)kk * ostride, scl(S[spad<T>(idx)], scale));
         }
     }
 }
@@ -143,7 +143,7 @@ __global__ void __launch_bounds__(ColTmaCfg<T, LOGL, C, E_>::THREADS, 1)
     k_colpass_tma(const __grid_constant__ CUtensorMap map, cpx<T> *__restrict__ out, long long ncols,
                   long long ld_out, long long odist, long long nbatch, const cpx<T> *__restrict__ tw,
                   const cpx<T> *__restrict__ tw_lo, const cpx<T> *__restrict__ tw_hi, int lo_bits, unsigned nmask,
-                  unsigned *err)
+                  unsigned *err, T scale)
 {
     using Cfg = ColTmaCfg<T, LOGL, C, E_>;
     using SP = typename Cfg::SP;
@@ -214,7 +214,7 @@ __global__ void __launch_bounds__(ColTmaCfg<T, LOGL, C, E_>::THREADS, 1)
                     val = twmul<INV>(val, wv);
                     if ((q & 3) == 3) asm volatile("" ::: "memory");
                 }
-                st_c(dst, val);
+                st_c(dst, scl(val, scale));
             }
             if constexpr (HERM) {
                 const long long W = 2 * (ncols - 1);
@@ -223,7 +223,7 @@ __global__ void __launch_bounds__(ColTmaCfg<T, LOGL, C, E_>::THREADS, 1)
 #pragma unroll
                     for (int q = 0; q < E; q++) {
                         const int i = t + q * G;
-                        st_c(mir + (long long)((N - i) & (N - 1)) * ld_out, conj(v[q]));
+                        st_c(mir + (long long)((N - i) & (N - 1)) * ld_out, scl(conj(v[q]), scale));
                     }
                 }
             }

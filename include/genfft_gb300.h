@@ -101,6 +101,12 @@ gfft_status gfft_plan_destroy(gfft_plan plan);
  * imaginary parts of the DC and Nyquist bins ignored (no counterpart in the
  * reference, whose RealFFT has no inverse, FFTReal.h:127-130). */
 gfft_status gfft_exec(gfft_plan plan, int inverse, void *out, const void *in, void *stream);
+/* gfft_exec with every output multiplied by `scale` inside the kernel that
+ * writes it (no extra pass): the norm= factors of torch.fft-style APIs
+ * (1/n, 1/sqrt(n)).  No counterpart in the reference, whose inverse is
+ * always unscaled (README.txt:28-31). */
+gfft_status gfft_exec_scaled(gfft_plan plan, int inverse, double scale, void *out, const void *in,
+                             void *stream);
 /* Adjoint (reverse-mode gradient) of the plan's transform in direction
  * `inverse`: grad_in = A^H grad_out with PyTorch's complex convention.
  * C2C / 2D / VERT: the conjugate-direction transform.  R2C forward: a C2R of
