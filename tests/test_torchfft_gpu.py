@@ -171,4 +171,4 @@ def test_exec_scaled_is_exec_times_scale(gfft, case):
     p.exec(y0, x, inv)
     p.exec(y1, x, inv, scale=s)
     torch.cuda.synchronize()
-    assert rel(y1, y0 * s) <= 1e-6 if dt == 0 else 1e-14, case
+    assert rel(y1, y0 * s) <= (1e-6 if dt == 0 else 1e-14), case
