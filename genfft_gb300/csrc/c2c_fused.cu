@@ -36,10 +36,16 @@ struct FusedCfg {
     static constexpr int TPC = SP::G >= 256 ? 1 : 256 / SP::G;
     static constexpr int THREADS = SP::G * TPC;
     static constexpr size_t SMEM = (size_t)SP::SMEM * TPC * sizeof(cpx<T>);
+    // four resident CTAs (64 registers a thread) where that costs no spill
+    // (fp32 n = 2^12 and n <= 2^8, ptxas -v), else three for CTAs of up to
+    // 256 threads (the residency the compiler picked unconstrained) and two
+    // for 512-thread CTAs
+    static constexpr int MIN_BLOCKS = (sizeof(T) == 4 && (LOGN == 12 || (LOGN >= 5 && LOGN <= 8))) ? 4
+                                    : THREADS <= 256 ? 3 : THREADS <= 512 ? 2 : 1;
 };
 
 template <typename T, int LOGN, bool INV>
-__global__ void __launch_bounds__(FusedCfg<T, LOGN>::THREADS)
+__global__ void __launch_bounds__(FusedCfg<T, LOGN>::THREADS, FusedCfg<T, LOGN>::MIN_BLOCKS)
     k_c2c_fused(const cpx<T> *__restrict__ in, cpx<T> *__restrict__ out, long long batch,
                 long long idist, long long odist, long long istride, long long ostride,
                 const cpx<T> *__restrict__ tw, T scale)
