@@ -23,7 +23,7 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "--expt-relaxed-constexpr", "-Xcompiler",
-              "-fPIC,-O3", f"-I{INCLUDE}"] + ARCH
+              "-fPIC,-O3", f"-I{INCLUDE}"] + ARCH + os.environ.get("GFFT_NVCC_EXTRA", "").split()
 
 
 def _nvcc() -> str:

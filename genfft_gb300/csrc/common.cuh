@@ -25,6 +25,40 @@ template <typename T>
 __device__ __forceinline__ cpx<T> operator+(cpx<T> a, cpx<T> b) { return {a.x + b.x, a.y + b.y}; }
 template <typename T>
 __device__ __forceinline__ cpx<T> operator-(cpx<T> a, cpx<T> b) { return {a.x - b.x, a.y - b.y}; }
+
+#ifndef GFFT_PACKED_F32
+#define GFFT_PACKED_F32 1
+#endif
+#if GFFT_PACKED_F32
+// fp32 complex add / subtract as one packed two-lane instruction
+// (add/sub.rn.f32x2, sm_100 family): both lanes of a butterfly at once
+template <>
+__device__ __forceinline__ cpx<float> operator+(cpx<float> a, cpx<float> b)
+{
+    cpx<float> d;
+    asm("{\n\t.reg .b64 ra, rb, rd;\n\t"
+        "mov.b64 ra, {%2, %3};\n\t"
+        "mov.b64 rb, {%4, %5};\n\t"
+        "add.rn.f32x2 rd, ra, rb;\n\t"
+        "mov.b64 {%0, %1}, rd;\n\t}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return d;
+}
+template <>
+__device__ __forceinline__ cpx<float> operator-(cpx<float> a, cpx<float> b)
+{
+    cpx<float> d;
+    asm("{\n\t.reg .b64 ra, rb, rd;\n\t"
+        "mov.b64 ra, {%2, %3};\n\t"
+        "mov.b64 rb, {%4, %5};\n\t"
+        "sub.rn.f32x2 rd, ra, rb;\n\t"
+        "mov.b64 {%0, %1}, rd;\n\t}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return d;
+}
+#endif
 template <typename T>
 __device__ __forceinline__ cpx<T> operator-(cpx<T> a) { return {-a.x, -a.y}; }
 
