@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstdint>
 #include <cstring>
 #include <map>
@@ -748,6 +749,32 @@ gfft_status gfft_separate_2x_real_fft(int dtype, int n, void *out1, void *out2, 
         check_ptr(out2, cplx_bytes(dtype), "out2");
         if (out1 == out2) fail(GFFT_ERR_ALIAS, "out1 and out2 must differ");
         check_cuda(launch_separate2x(dtype, in, out1, out2, n, (cudaStream_t)stream), "separate");
+    });
+}
+
+// ---- test hook (not declared in the public header) -------------------------
+// One persistent four-step launch (fp32, n = 2^16) whose only work items are
+// row tiles waiting on column tiles that are never scheduled: their bounded
+// dependency wait runs out after about one second, the kernel records
+// DEV_ERR_TMA_TIMEOUT in the device error word and every CTA returns.  It
+// writes nothing to `out`.  Lets a test check that no wait can hang and
+// that the context stays usable.
+gfft_status gfft_test_stalled_fourstep(void *out, const void *in, void *stream)
+{
+    GFFT_GUARD({
+        check_device();
+        gfft::C2CCore core;
+        core.init(GFFT_F32, 16, 1, 1);  // the persistent kernel
+        cudaError_t e = cudaSuccess;
+        try {
+            core.run_stalled(in, out, (cudaStream_t)stream);
+            e = cudaStreamSynchronize((cudaStream_t)stream);
+        } catch (...) {
+            core.release();
+            throw;
+        }
+        core.release();
+        check_cuda(e, "stalled four-step");
     });
 }
 

@@ -34,7 +34,7 @@ static const void *tile_table(int dtype, const TileKernel *k, int logl, int c)
 // ---------------------------------------------------------------------------
 // C2C
 
-void C2CCore::init(int dtype_, int logn_, long long batch_hint)
+void C2CCore::init(int dtype_, int logn_, long long batch_hint, int path)
 {
     dtype = dtype_;
     logn = logn_;
@@ -83,7 +83,8 @@ void C2CCore::init(int dtype_, int logn_, long long batch_hint)
     // n = 2^16 .. 2^19; the tile launches for 2^15, for 2^20 and above, and
     // for fp64
     const bool fs_default = dtype == GFFT_F32 && logn >= 16 && logn <= 19;
-    if (nvar > 0 && env_ll("GFFT_FS", fs_default ? 1 : 0) != 0) {
+    const bool use_fs = path >= 0 ? path == 1 : env_ll("GFFT_FS", fs_default ? 1 : 0) != 0;
+    if (nvar > 0 && use_fs) {
         // persistent four-step (the tile width / stage count GFFT_FS_CC /
         // GFFT_FS_NS name, else the rule below)
         fs = vars[0];
@@ -215,6 +216,37 @@ void C2CCore::run(int inverse, const void *in, void *out, long long batch, long 
         check_cuda(launch_rowpass(*krow, inverse, A / crow, nb, ws, dst, A, B, A, N, odist, tw_row, st, scale),
                    "launch row pass");
     }
+}
+
+void C2CCore::run_stalled(const void *in, void *out, cudaStream_t st) const
+{
+    if (algo != 3) fail(GFFT_ERR_UNSUPPORTED, "not a persistent four-step plan");
+    const size_t eb = cplx_bytes(dtype);
+    const long long A = 1LL << fs->la, B = 1LL << fs->lb;
+    const unsigned units = (unsigned)(eb / 8);
+    CUtensorMap map;
+    if (!make_tensor_map_3d(&map, in, (unsigned long long)B * units, (unsigned long long)A, 1,
+                            (unsigned long long)(B * eb), (unsigned long long)(A * B * eb), (unsigned)(fs->cc * units),
+                            (unsigned)fs->boxr))
+        fail(GFFT_ERR_ALIGN, "input not 16-byte aligned");
+    FourStepArgs a;
+    a.in = in;
+    a.out = out;
+    a.ws = ws;
+    a.batch = 0;  // no column tile is ever scheduled ...
+    a.idist = a.odist = A * B;
+    a.ctr = fs_ctr;
+    a.err = device_error_word();
+    a.tw_a = tw_a;
+    a.tw_b = tw_b;
+    a.tw_lo = tw_lo;
+    a.tw_hi = tw_hi;
+    a.lo_bits = lo_bits;
+    a.slots = 1;
+    a.lag = 1;  // ... but the row tiles of transform 0 are (phase 1)
+    a.nitems = 2 * (fs->nc + fs->nr);
+    a.scale = 1.0;
+    check_cuda(launch_fourstep(*fs, 0, map, a, fs_grid, st), "launch persistent four-step");
 }
 
 // ---------------------------------------------------------------------------

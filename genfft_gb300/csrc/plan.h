@@ -34,12 +34,17 @@ struct C2CCore {
     void *ws = nullptr;        // group * n (algo 2) or fs_slots * n (algo 3) elements
     size_t ws_bytes = 0;
 
-    void init(int dtype, int logn, long long batch_hint);
+    // path: -1 the measured default (or GFFT_FS), 1 the persistent
+    // four-step kernel, 0 the tile launches
+    void init(int dtype, int logn, long long batch_hint, int path = -1);
     void release();
     int launches(long long batch) const;
     // strides in complex elements; four-step needs unit element strides
     void run(int inverse, const void *in, void *out, long long batch, long long idist, long long odist,
              long long istride, long long ostride, cudaStream_t st, double scale = 1.0) const;
+    // persistent four-step only: one launch whose row tiles wait on column
+    // tiles that are never scheduled (the bounded wait must run out)
+    void run_stalled(const void *in, void *out, cudaStream_t st) const;
 };
 
 // Column FFTs of length 2^logl over ncols columns (tile kernels).

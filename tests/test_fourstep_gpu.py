@@ -105,3 +105,33 @@ def test_in_place_and_old_path(gfft, oracle):
 
 def test_no_device_error(gfft):
     assert gfft.device_error() == 0
+
+
+def test_fp64_persistent_schedules(gfft, oracle):
+    """fp64 through the persistent kernel (the tile launches are its
+    default): ring shapes agree bit for bit and meet the fp64 bound."""
+    import torch
+    n, batch = 1 << 16, 5
+    g = torch.Generator(device="cuda").manual_seed(64)
+    x = torch.randn(batch, n, dtype=torch.complex128, device="cuda", generator=g)
+    outs = []
+    for env in ({}, {"GFFT_FS_SLOTS": 1, "GFFT_FS_LAG": 0}, {"GFFT_FS_SLOTS": 4, "GFFT_FS_LAG": 2}):
+        old = {k: os.environ.get(k) for k in ("GFFT_FS", *env)}
+        os.environ.update({"GFFT_FS": "1", **{k: str(v) for k, v in env.items()}})
+        try:
+            p = gfft.Plan(gfft.KIND_C2C, gfft.F64, n, 0, batch)
+        finally:
+            for k, v in old.items():
+                if v is None:
+                    os.environ.pop(k, None)
+                else:
+                    os.environ[k] = v
+        assert p.launches() == 1
+        y = torch.empty_like(x)
+        p.exec(y, x)
+        torch.cuda.synchronize()
+        outs.append(y.cpu().numpy())
+    exact = oracle.fft64(x.cpu().numpy())
+    assert oracle.rel_rms(outs[0], exact) <= 1e-15 * 16
+    for o in outs[1:]:
+        assert np.array_equal(o, outs[0])
