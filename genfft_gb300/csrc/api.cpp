@@ -394,8 +394,13 @@ static void exec_host(gfft_plan_s &p, int inverse, void *out, const void *in)
     std::lock_guard<std::mutex> lk(p.host_mu);
     size_t ib, ob;
     io_item_bytes(p, &ib, &ob);
-    // chunks of about 64 MB, at least one transform
-    long long per = std::max<long long>(1, (long long)((64u << 20) / std::max<size_t>(std::max(ib, ob), 1)));
+    // chunks of about 64 MB (GFFT_HOST_CHUNK_MB), at least one transform
+    static const long long chunk = [] {
+        const char *v = std::getenv("GFFT_HOST_CHUNK_MB");
+        const long long mb = (v && *v) ? std::atoll(v) : 64;
+        return std::max<long long>(1, mb) << 20;
+    }();
+    long long per = std::max<long long>(1, chunk / (long long)std::max<size_t>(std::max(ib, ob), 1));
     per = std::min(per, d.batch);
     if (!p.stage[0] || p.stage_bytes_in < per * ib || p.stage_bytes_out < per * ob) {
         for (int i = 0; i < 3; i++) {
