@@ -293,6 +293,16 @@ void R2CCore::init(int dtype_, int logn_, int half_, long long batch_hint)
                           [d, lh](void *buf) { r2c_twiddle_fill(d, lh, buf); });
         return;
     }
+    // the DIT fused into the row pass of a four-step split of n/2 (fp32)
+    const RowDitKernel *k = rowdit_find(dtype, lh - lh / 2);
+    if (k && env_ll("GFFT_R2C_FUSED_DIT", 1) != 0) {
+        c2c.init(dtype, lh, batch_hint, 0);  // column pass, tables and workspace of the tile path
+        rowdit = k;
+        tw_rowdit = cached_table("rowdit/" + std::to_string(d) + "/" + std::to_string(k->logb), d, k->twcount,
+                                 [k](void *buf) { k->fill(buf); });
+        algo = 3;
+        return;
+    }
     algo = 2;
     c2c.init(dtype, lh, batch_hint);
 }
@@ -300,6 +310,7 @@ void R2CCore::init(int dtype_, int logn_, int half_, long long batch_hint)
 int R2CCore::launches(long long batch) const
 {
     if (algo == 2) return c2c.launches(batch) + 1;
+    if (algo == 3) return c2c.launches(batch);
     return 1;
 }
 
@@ -312,6 +323,21 @@ void R2CCore::run(const void *in, void *out, long long batch, long long idist, l
     } else if (algo == 1) {
         check_cuda(launch_r2c_fused(dtype, logn - 1, mode, in, out, batch, idist, odist, tw, dtw, st, scale),
                    "launch fused R2C");
+    } else if (algo == 3 && mode == 0) {
+        // column pass of the n/2-point split into the workspace, then the
+        // row pass with the DIT adjustment fused, straight into the spectrum
+        const long long A = 1LL << c2c.logA, B = 1LL << c2c.logB, N = A * B;
+        const size_t eb = cplx_bytes(dtype);
+        for (long long g0 = 0; g0 < batch; g0 += c2c.group) {
+            const long long nb = std::min(c2c.group, batch - g0);
+            const char *src = static_cast<const char *>(in) + (size_t)(g0 * (idist / 2)) * eb;
+            char *dst = static_cast<char *>(out) + (size_t)(g0 * odist) * eb;
+            check_cuda(launch_colpass(*c2c.kcol, 0, B / c2c.ccol, nb, src, c2c.ws, B, B, B, idist / 2, N, c2c.tw_col,
+                                      c2c.tw_lo, c2c.tw_hi, c2c.lo_bits, (unsigned)(N - 1), st),
+                       "launch column pass");
+            check_cuda(launch_rowpass_dit(*rowdit, c2c.ws, dst, A, nb, N, odist, tw_rowdit, dtw, st, scale),
+                       "launch row pass with DIT");
+        }
     } else {
         const long long H = 1LL << (logn - 1);
         // n reals are n/2 complex; transform them into the output buffer,

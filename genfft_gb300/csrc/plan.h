@@ -57,12 +57,31 @@ struct ColCore {
              long long batch, long long idist, long long odist, cudaStream_t st, double scale = 1.0) const;
 };
 
+// Row pass of a four-step real-input transform with the DIT adjustment
+// fused in (real_4step.cu)
+struct RowDitKernel {
+    const void *fn = nullptr;
+    int threads = 0;
+    size_t smem = 0;
+    int ch = 0, logb = 0;  // rows per half-block, log2 row length
+    size_t twcount = 0;
+    void (*fill)(void *) = nullptr;
+};
+const RowDitKernel *rowdit_find(int dtype, int logb);
+cudaError_t launch_rowpass_dit(const RowDitKernel &k, const void *in, void *out, long long A, long long batch,
+                               long long idist, long long odist, const void *tw, const void *dtw, cudaStream_t st,
+                               double scale = 1.0);
+
 // Real-input 1D transform of n = 2^logn reals (RealFFT<T>::forward).
 // mode: 0 half spectrum, 1 full spectrum, 2 half with doubled interior bins
 struct R2CCore {
     int dtype = 0, logn = 0, half = 1;
-    int algo = 0;  // 0 n == 1, 1 fused, 2 C2C(n/2) + DIT pass
+    // 0 n == 1, 1 fused, 2 C2C(n/2) + DIT pass, 3 four-step column pass +
+    // row pass with the DIT fused (half spectrum; other modes as 2)
+    int algo = 0;
     const void *tw = nullptr, *dtw = nullptr;
+    const RowDitKernel *rowdit = nullptr;
+    const void *tw_rowdit = nullptr;
     C2CCore c2c;
     void init(int dtype, int logn, int half, long long batch_hint);
     void release() { c2c.release(); }

@@ -19,6 +19,7 @@
 
 #include "internal.h"
 #include "plan.h"
+#include "dit.cuh"
 #include "stockham.cuh"
 #include "twiddle.h"
 
@@ -41,17 +42,6 @@ struct R2CCfg {
     static constexpr int SMEM_T = spad_size<T>(SP::N);
     static constexpr size_t SMEM = (size_t)SMEM_T * TPC * sizeof(cpx<T>);
 };
-
-// F_k from Z_k, Z_j and the DIT twiddle t_k = (sin, cos) = dtw[k]
-template <typename T>
-__device__ __forceinline__ cpx<T> dit_value(cpx<T> zk, cpx<T> zj, cpx<T> t)
-{
-    const T h = (T)0.5;
-    const cpx<T> e{(zk.x + zj.x) * h, (zk.y - zj.y) * h};
-    const cpx<T> o{(zk.x - zj.x) * h, (zk.y + zj.y) * h};
-    const cpx<T> to = cmul(t, o);
-    return {e.x - to.x, e.y - to.y};
-}
 
 // output modes of the real-input kernels
 enum R2CMode { R2C_HALF = 0, R2C_FULL = 1, R2C_HALF_X2 = 2 };

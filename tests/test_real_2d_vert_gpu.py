@@ -252,3 +252,36 @@ def test_alias_errors(gfft):
     with pytest.raises(gfft.GFFTError) as e:
         p.exec_ptr(out.data_ptr(), xr.data_ptr(), True, 0)
     assert e.value.name == "GFFT_ERR_UNSUPPORTED"
+
+
+@pytest.mark.parametrize("logn", [16, 17, 18, 20, 22, 24])
+def test_real_fft_fused_dit_row_pass(gfft, logn):
+    """Half-spectrum R2C above the fused limit with the DIT adjustment fused
+    into the four-step row pass (row lengths 2^8 .. 2^12), against an FP64
+    transform and against the separate DIT pass (GFFT_R2C_FUSED_DIT=0)."""
+    import os
+    import torch
+    n = 1 << logn
+    batch = 3 if logn <= 20 else 1
+    g = torch.Generator(device="cuda").manual_seed(logn)
+    x = torch.rand(batch, n, dtype=torch.float32, device="cuda", generator=g) * 2 - 1
+    outs = []
+    for fused in ("1", "0"):
+        old = os.environ.get("GFFT_R2C_FUSED_DIT")
+        os.environ["GFFT_R2C_FUSED_DIT"] = fused
+        try:
+            p = gfft.Plan(gfft.KIND_R2C, gfft.F32, n, 0, batch, gfft.FLAG_HALF_SPECTRUM)
+        finally:
+            if old is None:
+                os.environ.pop("GFFT_R2C_FUSED_DIT")
+            else:
+                os.environ["GFFT_R2C_FUSED_DIT"] = old
+        y = torch.full((batch, n // 2 + 1), float("nan"), dtype=torch.complex64, device="cuda")
+        p.exec(y, x)
+        torch.cuda.synchronize()
+        outs.append(host(y))
+    ref = np.fft.rfft(x.cpu().numpy().astype(np.float64))
+    for got in outs:
+        assert np.all(np.isfinite(got.view(np.float32)))  # every bin written
+        assert np.linalg.norm(got - ref) / np.linalg.norm(ref) <= bound(np.float32, n)
+    assert np.linalg.norm(outs[0] - outs[1]) / np.linalg.norm(ref) <= 1e-6
