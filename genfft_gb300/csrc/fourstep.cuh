@@ -29,6 +29,7 @@
 // except the rare COL slot-free check.  Every wait is bounded.
 #pragma once
 
+#include "dit.cuh"
 #include "fourstep.h"
 #include "tiles.cuh"
 #include "tma.cuh"
@@ -54,6 +55,9 @@ struct FourStepCfg {
     static constexpr int CR = CT / SPB::G;         // rows per ROW tile
     static constexpr long long A = 1LL << LA, B = 1LL << LB, N = A * B;
     static constexpr int NC = (int)(B / CC), NR = (int)(A / CR);
+    // real-input mode: row items pair CH = CR/2 rows with their mirrors
+    // (A / CR pair items) plus one item for the self-paired row 0
+    static constexpr int CH = CR / 2, NRP = (int)(A / CR) + 1;
     static constexpr int BOXR = A < 256 ? (int)A : 256;  // rows per tensor box
     // COL stage: A rows of CC landed by the tensor copies, then the padded
     // column-major exchange layout of tiles.cuh
@@ -129,7 +133,13 @@ __device__ __forceinline__ bool fs_wait_geq(const int *p, int target, const int 
     return true;
 }
 
-template <typename T, int LA, int LB, int CC, int E_, int NS_, bool INV>
+// DIT: the real-input transform (forward, half spectrum): the input is the
+// n reals read as N = n/2 complex values, and the row items apply the DIT
+// adjustment (dit.cuh) to bin pairs (k, N - k) before storing the N + 1
+// bins.  Bin k = k1 + A k2 pairs with row A - k1, column B - 1 - k2 (row 0
+// with itself, column B - k2), so a row item transforms CH rows and their
+// mirrors together.
+template <typename T, int LA, int LB, int CC, int E_, int NS_, bool INV, bool DIT = false>
 __global__ void __launch_bounds__(FourStepCfg<T, LA, LB, CC, E_, NS_>::THREADS,
                                   FourStepCfg<T, LA, LB, CC, E_, NS_>::MIN_BLOCKS)
     k_fourstep(const __grid_constant__ CUtensorMap map, const FourStepArgs a)
@@ -138,7 +148,10 @@ __global__ void __launch_bounds__(FourStepCfg<T, LA, LB, CC, E_, NS_>::THREADS,
     using SPA = typename Cfg::SPA;
     using SPB = typename Cfg::SPB;
     constexpr int EA = SPA::E, GA = SPA::G, EB = SPB::E, GB = SPB::G;
-    constexpr int CT = Cfg::CT, CR = Cfg::CR, NC = Cfg::NC, NR = Cfg::NR, NS = Cfg::NS;
+    constexpr int CT = Cfg::CT, CR = Cfg::CR, NC = Cfg::NC, NS = Cfg::NS;
+    constexpr int NR = DIT ? Cfg::NRP : Cfg::NR, CH = Cfg::CH;
+    static_assert(!DIT || (CH >= 1 && !INV), "real-input mode: forward, at least two rows per item");
+    static_assert(!DIT || (sizeof(T) == 4 && Cfg::ROWP >= SPB::N + SPB::N / 16), "real-input mode: padded fp32 rows");
     constexpr long long A = Cfg::A, B = Cfg::B, N = Cfg::N;
     constexpr int UNITS = (int)sizeof(cpx<T>) / 8;  // 8-byte tensor elements per complex value
     extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -221,13 +234,30 @@ __global__ void __launch_bounds__(FourStepCfg<T, LA, LB, CC, E_, NS_>::THREADS,
                 }
                 __threadfence();
                 fence_proxy_async_global();
-                const long long row0 = (long long)(j - NC) * CR;
-                const cpx<T> *src = static_cast<const cpx<T> *>(a.ws) + (long long)slot * N + row0 * B;
+                const cpx<T> *slot_base = static_cast<const cpx<T> *>(a.ws) + (long long)slot * N;
                 item_of[st] = item;
-                mbar_arrive_expect_tx(&full[st], (uint32_t)(CR * B * sizeof(cpx<T>)));
+                if (DIT) {
+                    const int r = j - NC;
+                    if (r < NR - 1) {
+                        // rows 1 + CH r .. + CH - 1, then their mirrors A - CH r - CH .. A - CH r - 1
+                        mbar_arrive_expect_tx(&full[st], (uint32_t)(2 * CH * B * sizeof(cpx<T>)));
+                        bulk_load(S, slot_base + (1 + (long long)CH * r) * B, (uint32_t)(CH * B * sizeof(cpx<T>)),
+                                  &full[st]);
+                        bulk_load(S + (size_t)CH * B, slot_base + (A - (long long)CH * r - CH) * B,
+                                  (uint32_t)(CH * B * sizeof(cpx<T>)), &full[st]);
+                    } else {  // row 0
+                        mbar_arrive_expect_tx(&full[st], (uint32_t)(B * sizeof(cpx<T>)));
+                        bulk_load(S, slot_base, (uint32_t)(B * sizeof(cpx<T>)), &full[st]);
+                    }
+                } else {
+                    const long long row0 = (long long)(j - NC) * CR;
+                    const cpx<T> *src = slot_base + row0 * B;
+                    mbar_arrive_expect_tx(&full[st], (uint32_t)(CR * B * sizeof(cpx<T>)));
 #pragma unroll 1
-                for (int s = 0; s < CR; s++)
-                    bulk_load(S + (size_t)s * B, src + (long long)s * B, (uint32_t)(B * sizeof(cpx<T>)), &full[st]);
+                    for (int s = 0; s < CR; s++)
+                        bulk_load(S + (size_t)s * B, src + (long long)s * B, (uint32_t)(B * sizeof(cpx<T>)),
+                                  &full[st]);
+                }
             }
             k++;
         }
@@ -308,6 +338,78 @@ __global__ void __launch_bounds__(FourStepCfg<T, LA, LB, CC, E_, NS_>::THREADS,
             const long long t = p - a.lag;
             const int slot = (int)(t % a.slots);
             const int s = tid / GB, tt = tid - s * GB;
+            if constexpr (DIT) {
+                // ---- real-input row item: CH rows and their mirrors (or row 0)
+                const int r = j - NC;
+                const bool row0 = r == NR - 1;
+                const cpx<T> *slot_base = static_cast<const cpx<T> *>(a.ws) + (long long)slot * N;
+                {
+                    // drop the copied rows' L2 lines without a write-back
+                    auto drop = [tid](const cpx<T> *base, long long elems) {
+                        const char *c = reinterpret_cast<const char *>(base);
+                        const int lines = (int)(elems * (long long)sizeof(cpx<T>) / 128);
+                        for (int i = tid; i < lines; i += CT)
+                            asm volatile("discard.global.L2 [%0], 128;" ::"l"(c + (size_t)i * 128) : "memory");
+                    };
+                    if (row0) {
+                        drop(slot_base, B);
+                    } else {
+                        drop(slot_base + (1 + (long long)CH * r) * B, (long long)CH * B);
+                        drop(slot_base + (A - (long long)CH * r - CH) * B, (long long)CH * B);
+                    }
+                }
+                cpx<T> v[EB];
+#pragma unroll
+                for (int q = 0; q < EB; q++) v[q] = S[s * B + tt + q * GB];
+                bar_compute(CT);
+                if (tid == 0) {
+                    __threadfence();
+                    atomicAdd(row_done + slot, 1);
+                }
+                cpx<T> *my = S + s * Cfg::ROWP;
+                stockham_run<T, LB, E_, false, TwShared>(
+                    v, tt, [my](int i) -> cpx<T> & { return my[spad<T>(i)]; }, twb, []() { bar_compute(CT); });
+                bar_compute(CT);
+                // Z tile: slot s, column k2 rotated by s * ZROT (so that the
+                // CH slots a warp reads at once fall on different banks), then
+                // padded like the exchange
+                constexpr int ZROT = CH >= 2 ? 32 / CH : 0;
+                auto zpos = [](int slot_, int k2) {
+                    const int c = (k2 + slot_ * ZROT) & ((int)B - 1);
+                    return slot_ * Cfg::ROWP + c + (c >> 4);
+                };
+#pragma unroll
+                for (int q = 0; q < EB; q++) S[zpos(s, tt + q * GB)] = v[q];
+                bar_compute(CT);
+                auto Z = [S, zpos](int slot_, int k2) { return S[zpos(slot_, k2)]; };
+                cpx<T> *dst = static_cast<cpx<T> *>(a.out) + t * a.odist;
+                const cpx<T> *dtw = static_cast<const cpx<T> *>(a.dtw);
+                const T scale = (T)a.scale;
+                if (!row0) {
+                    // lo slot s2 (row 1 + CH r + s2) pairs with hi slot
+                    // 2 CH - 1 - s2 (row A - 1 - CH r - s2), column B - 1 - k2;
+                    // consecutive threads take consecutive rows: runs of CH bins
+                    for (int idx = tid; idx < CH * (int)B; idx += CT) {
+                        const int s2 = idx % CH, k2 = idx / CH;
+                        const long long k = 1 + (long long)CH * r + s2 + A * k2, jj = N - k;
+                        const cpx<T> zk = Z(s2, k2), zj = Z(2 * CH - 1 - s2, (int)B - 1 - k2);
+                        stcs_c(dst + k, scl(dit_value(zk, zj, ldg_c(dtw + k)), scale));
+                        stcs_c(dst + jj, scl(dit_value(zj, zk, ldg_c(dtw + jj)), scale));
+                    }
+                } else {
+                    // row 0: bins A k2 and A (B - k2), k2 = 0 .. B/2 (k2 = 0 also
+                    // gives the Nyquist bin N)
+                    for (int k2 = tid; k2 <= (int)B / 2; k2 += CT) {
+                        const long long k = A * k2, jj = N - k;
+                        const cpx<T> zk = Z(0, k2), zj = Z(0, ((int)B - k2) & ((int)B - 1));
+                        stcs_c(dst + k, scl(dit_value(zk, zj, ldg_c(dtw + k)), scale));
+                        stcs_c(dst + jj, scl(dit_value(zj, zk, ldg_c(dtw + jj)), scale));
+                    }
+                }
+                bar_compute(CT);
+                if (tid == 0) mbar_arrive(&empty[st]);
+                continue;
+            }
             const long long row0 = (long long)(j - NC) * CR;
             // the rows are in shared memory: drop their L2 lines without a
             // write-back (the slot is rewritten before it is read again),

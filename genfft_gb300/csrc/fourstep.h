@@ -23,15 +23,18 @@ struct FourStepArgs {
     int slots, lag;
     int nitems;
     double scale;             // applied to every output (norm= scaling)
+    const void *dtw;          // real-input mode: the DIT twiddles t_k, k = 0 .. N
 };
 
 struct FourStepKernel {
     const void *fwd = nullptr, *inv = nullptr;
+    const void *dit = nullptr;  // real-input (forward, DIT fused) version, or null
     int threads = 0;
     size_t smem = 0;
     int la = 0, lb = 0;      // N = 2^la * 2^lb: column length A, row length B
     int cc = 0, cr = 0;      // columns per COL tile, rows per ROW tile
     int nc = 0, nr = 0;      // tiles per transform
+    int nrp = 0;             // row items per transform in real-input mode (A / cr + 1)
     int boxr = 0;            // rows per tensor box of a COL tile
     int ns = 0;              // shared-memory stages
     size_t twa = 0, twb = 0; // Stockham table sizes (complex elements)
@@ -49,9 +52,11 @@ void fourstep_schedule(size_t bytes, long long batch, int grid, int depth, int i
                        int *lag);
 
 // `map` is the 3D tensor map of the input (8-byte units x rows x batch)
+// (dit: the real-input version, k.dit)
 cudaError_t launch_fourstep(const FourStepKernel &k, int inverse, const CUtensorMap &map, const FourStepArgs &a,
-                            int grid, cudaStream_t st);
-// CTAs of kernel k that run at once on the current device
-int fourstep_grid(const FourStepKernel &k);
+                            int grid, cudaStream_t st, bool dit = false);
+// CTAs of kernel k (or of its real-input version) that run at once on the
+// current device
+int fourstep_grid(const FourStepKernel &k, bool dit = false);
 
 }  // namespace gfft

@@ -86,37 +86,39 @@ void fourstep_schedule(size_t bytes, long long batch, int grid, int depth, int i
     *lag = lg;
 }
 
-int fourstep_grid(const FourStepKernel &k)
+int fourstep_grid(const FourStepKernel &k, bool dit)
 {
+    const void *const main_fn = dit ? k.dit : k.fwd;
     static std::mutex mu;
     static std::map<std::pair<int, const void *>, int> cache;
     int dev = 0;
     cudaGetDevice(&dev);
     std::lock_guard<std::mutex> lk(mu);
-    auto it = cache.find({dev, k.fwd});
+    auto it = cache.find({dev, main_fn});
     if (it != cache.end()) return it->second;
-    for (const void *fn : {k.fwd, k.inv})
-        if (k.smem > 48 * 1024)
+    for (const void *fn : {k.fwd, k.inv, k.dit})
+        if (fn && k.smem > 48 * 1024)
             check_cuda(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k.smem),
                        "four-step shared memory opt-in");
     int per_sm = 0, sms = 0;
-    check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k.fwd, k.threads, k.smem), "occupancy");
+    check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, main_fn, k.threads, k.smem), "occupancy");
     check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
     const int g = std::max(1, per_sm) * sms;
-    cache[{dev, k.fwd}] = g;
+    cache[{dev, main_fn}] = g;
     return g;
 }
 
 cudaError_t launch_fourstep(const FourStepKernel &k, int inverse, const CUtensorMap &map, const FourStepArgs &a,
-                            int grid, cudaStream_t st)
+                            int grid, cudaStream_t st, bool dit)
 {
+    if (dit && !k.dit) return cudaErrorInvalidValue;
     cudaError_t e = cudaMemsetAsync(a.ctr, 0, (size_t)(2 + 2 * a.slots) * sizeof(int), st);
     if (e != cudaSuccess) return e;
     FourStepArgs args = a;
     CUtensorMap m = map;
     void *p[] = {&m, &args};
     const int g = std::max(1, std::min(grid, a.nitems));
-    return cudaLaunchKernel(inverse ? k.inv : k.fwd, dim3((unsigned)g), dim3(k.threads), p, k.smem, st);
+    return cudaLaunchKernel(dit ? k.dit : inverse ? k.inv : k.fwd, dim3((unsigned)g), dim3(k.threads), p, k.smem, st);
 }
 
 }  // namespace gfft

@@ -31,6 +31,8 @@ struct FourStepReg {
         FourStepKernel k;
         k.fwd = (const void *)&k_fourstep<T, LA, LB, CC, E, NS, false>;
         k.inv = (const void *)&k_fourstep<T, LA, LB, CC, E, NS, true>;
+        if constexpr (sizeof(T) == 4 && Cfg::CR >= 2 && Cfg::SPB::P > 1)
+            k.dit = (const void *)&k_fourstep<T, LA, LB, CC, E, NS, false, true>;
         k.threads = Cfg::THREADS;
         k.smem = Cfg::SMEM;
         k.la = LA;
@@ -39,6 +41,7 @@ struct FourStepReg {
         k.cr = Cfg::CR;
         k.nc = Cfg::NC;
         k.nr = Cfg::NR;
+        k.nrp = Cfg::NRP;
         k.boxr = Cfg::BOXR;
         k.ns = NS;
         k.twa = (size_t)StockhamPlan<T, LA, E>::TW;

@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <cstdlib>
 #include <string>
+#include <vector>
 
 #include "plan.h"
 #include "twiddle.h"
@@ -34,7 +35,7 @@ static const void *tile_table(int dtype, const TileKernel *k, int logl, int c)
 // ---------------------------------------------------------------------------
 // C2C
 
-void C2CCore::init(int dtype_, int logn_, long long batch_hint, int path)
+void C2CCore::init(int dtype_, int logn_, long long batch_hint, int path, bool real_rows)
 {
     dtype = dtype_;
     logn = logn_;
@@ -84,6 +85,15 @@ void C2CCore::init(int dtype_, int logn_, long long batch_hint, int path)
     // for fp64
     const bool fs_default = dtype == GFFT_F32 && logn >= 16 && logn <= 19;
     const bool use_fs = path >= 0 ? path == 1 : env_ll("GFFT_FS", fs_default ? 1 : 0) != 0;
+    std::vector<const FourStepKernel *> dit_vars;
+    if (real_rows) {
+        // only the variants with a real-input version
+        for (int i = 0; i < nvar; i++)
+            if (vars[i]->dit) dit_vars.push_back(vars[i]);
+        vars = dit_vars.data();
+        nvar = (int)dit_vars.size();
+        if (!nvar) fail(GFFT_ERR_UNSUPPORTED, "no real-input four-step kernel for this length");
+    }
     if (nvar > 0 && use_fs) {
         // persistent four-step (the tile width / stage count GFFT_FS_CC /
         // GFFT_FS_NS name, else the rule below)
@@ -95,6 +105,19 @@ void C2CCore::init(int dtype_, int logn_, long long batch_hint, int path)
                     fs = vars[i];
                     break;
                 }
+        } else if (real_rows) {
+            // real input: row items of 8 or more rows (runs of 4+ bins per
+            // store) with 256 compute threads, else the most rows per item
+            const FourStepKernel *best = nullptr;
+            for (int i = 0; i < nvar; i++)
+                if (vars[i]->threads == 256 + 32 && vars[i]->cr >= 8) {
+                    best = vars[i];
+                    break;
+                }
+            if (!best)
+                for (int i = 0; i < nvar; i++)
+                    if (!best || vars[i]->cr > best->cr) best = vars[i];
+            fs = best;
         } else {
             // 256 compute threads (two or three CTAs per SM) with column
             // runs of 64 bytes or more, else the widest tile
@@ -110,9 +133,11 @@ void C2CCore::init(int dtype_, int logn_, long long batch_hint, int path)
                             k->twa, [k](void *buf) { k->fill_a(buf); });
         tw_b = cached_table("fs/" + std::to_string(d) + "/" + std::to_string(l_b) + "/" + std::to_string(k->twb), d,
                             k->twb, [k](void *buf) { k->fill_b(buf); });
-        fs_grid = fourstep_grid(*fs);
+        fs_real = real_rows;
+        fs_nr = real_rows ? fs->nrp : fs->nr;
+        fs_grid = fourstep_grid(*fs, real_rows);
         fourstep_schedule((size_t)N * cplx_bytes(dtype), std::max<long long>(1, batch_hint), fs_grid, fs->ns + 1,
-                          fs->nc + fs->nr, &fs_slots, &fs_lag);
+                          fs->nc + fs_nr, &fs_slots, &fs_lag);
         group = fs_slots;  // the tile path reuses the ring as its workspace
         ws_bytes = (size_t)fs_slots * (size_t)N * cplx_bytes(dtype);
         check_cuda(cudaMalloc(&ws, ws_bytes), "cudaMalloc(workspace)");
@@ -139,15 +164,18 @@ void C2CCore::release()
 }
 
 // transforms per persistent launch: the item count stays far below 2^31
-static long long fs_chunk(const FourStepKernel &k, int lag)
+static long long fs_chunk(int items_per_transform, int lag)
 {
-    return std::max<long long>(1, (1LL << 30) / (k.nc + k.nr) - lag);
+    return std::max<long long>(1, (1LL << 30) / items_per_transform - lag);
 }
 
 int C2CCore::launches(long long batch) const
 {
     if (algo == 1) return 1;
-    if (algo == 3) return (int)((batch + fs_chunk(*fs, fs_lag) - 1) / fs_chunk(*fs, fs_lag));
+    if (algo == 3) {
+        const long long chunk = fs_chunk(fs->nc + fs_nr, fs_lag);
+        return (int)((batch + chunk - 1) / chunk);
+    }
     return 2 * (int)((batch + group - 1) / group);
 }
 
@@ -161,46 +189,7 @@ void C2CCore::run(int inverse, const void *in, void *out, long long batch, long 
     }
     if (istride != 1 || ostride != 1)
         fail(GFFT_ERR_UNSUPPORTED, "lengths above the fused limit need unit element strides");
-    if (algo == 3) {
-        const size_t eb = cplx_bytes(dtype);
-        const long long chunk = fs_chunk(*fs, fs_lag);
-        const long long A = 1LL << fs->la, B = 1LL << fs->lb;
-        const unsigned units = (unsigned)(eb / 8);
-        bool launched = false;
-        for (long long b0 = 0; b0 < batch; b0 += chunk) {
-            const long long nb = std::min(chunk, batch - b0);
-            FourStepArgs a;
-            a.in = static_cast<const char *>(in) + (size_t)(b0 * idist) * eb;
-            a.out = static_cast<char *>(out) + (size_t)(b0 * odist) * eb;
-            // the input as [batch][A rows][B columns] of 8-byte units
-            CUtensorMap map;
-            if (!make_tensor_map_3d(&map, a.in, (unsigned long long)B * units, (unsigned long long)A,
-                                    (unsigned long long)nb, (unsigned long long)(B * eb),
-                                    (unsigned long long)((nb > 1 ? idist : A * B) * eb), (unsigned)(fs->cc * units),
-                                    (unsigned)fs->boxr)) {
-                if (launched) fail(GFFT_ERR_ALIGN, "input chunk not 16-byte aligned");
-                break;  // unaligned input: the tile path below
-            }
-            a.ws = ws;
-            a.batch = nb;
-            a.idist = idist;
-            a.odist = odist;
-            a.ctr = fs_ctr;
-            a.err = device_error_word();
-            a.tw_a = tw_a;
-            a.tw_b = tw_b;
-            a.tw_lo = tw_lo;
-            a.tw_hi = tw_hi;
-            a.lo_bits = lo_bits;
-            a.slots = fs_slots;
-            a.lag = fs_lag;
-            a.nitems = (int)((nb + fs_lag) * (fs->nc + fs->nr));
-            a.scale = scale;
-            check_cuda(launch_fourstep(*fs, inverse, map, a, fs_grid, st), "launch persistent four-step");
-            launched = true;
-        }
-        if (launched) return;
-    }
+    if (algo == 3 && !fs_real && run_persistent(inverse, in, out, batch, idist, odist, st, scale)) return;
     const long long A = 1LL << logA, B = 1LL << logB, N = A * B;
     const size_t eb = cplx_bytes(dtype);
     const unsigned nmask = (unsigned)(N - 1);
@@ -216,6 +205,48 @@ void C2CCore::run(int inverse, const void *in, void *out, long long batch, long 
         check_cuda(launch_rowpass(*krow, inverse, A / crow, nb, ws, dst, A, B, A, N, odist, tw_row, st, scale),
                    "launch row pass");
     }
+}
+
+bool C2CCore::run_persistent(int inverse, const void *in, void *out, long long batch, long long idist,
+                             long long odist, cudaStream_t st, double scale, const void *dtw) const
+{
+    const size_t eb = cplx_bytes(dtype);
+    const long long chunk = fs_chunk(fs->nc + fs_nr, fs_lag);
+    const long long A = 1LL << fs->la, B = 1LL << fs->lb;
+    const unsigned units = (unsigned)(eb / 8);
+    for (long long b0 = 0; b0 < batch; b0 += chunk) {
+        const long long nb = std::min(chunk, batch - b0);
+        FourStepArgs a;
+        a.in = static_cast<const char *>(in) + (size_t)(b0 * idist) * eb;
+        a.out = static_cast<char *>(out) + (size_t)(b0 * odist) * eb;
+        // the input as [batch][A rows][B columns] of 8-byte units
+        CUtensorMap map;
+        if (!make_tensor_map_3d(&map, a.in, (unsigned long long)B * units, (unsigned long long)A,
+                                (unsigned long long)nb, (unsigned long long)(B * eb),
+                                (unsigned long long)((nb > 1 ? idist : A * B) * eb), (unsigned)(fs->cc * units),
+                                (unsigned)fs->boxr)) {
+            if (b0 > 0) fail(GFFT_ERR_ALIGN, "input chunk not 16-byte aligned");
+            return false;
+        }
+        a.ws = ws;
+        a.batch = nb;
+        a.idist = idist;
+        a.odist = odist;
+        a.ctr = fs_ctr;
+        a.err = device_error_word();
+        a.tw_a = tw_a;
+        a.tw_b = tw_b;
+        a.tw_lo = tw_lo;
+        a.tw_hi = tw_hi;
+        a.lo_bits = lo_bits;
+        a.slots = fs_slots;
+        a.lag = fs_lag;
+        a.nitems = (int)((nb + fs_lag) * (fs->nc + fs_nr));
+        a.scale = scale;
+        a.dtw = dtw;
+        check_cuda(launch_fourstep(*fs, inverse, map, a, fs_grid, st, fs_real), "launch persistent four-step");
+    }
+    return true;
 }
 
 void C2CCore::run_stalled(const void *in, void *out, cudaStream_t st) const
@@ -246,6 +277,7 @@ void C2CCore::run_stalled(const void *in, void *out, cudaStream_t st) const
     a.lag = 1;  // ... but the row tiles of transform 0 are (phase 1)
     a.nitems = 2 * (fs->nc + fs->nr);
     a.scale = 1.0;
+    a.dtw = nullptr;
     check_cuda(launch_fourstep(*fs, 0, map, a, fs_grid, st), "launch persistent four-step");
 }
 
@@ -296,10 +328,27 @@ void R2CCore::init(int dtype_, int logn_, int half_, long long batch_hint)
     // the DIT fused into the row pass of a four-step split of n/2 (fp32)
     const RowDitKernel *k = rowdit_find(dtype, lh - lh / 2);
     if (k && env_ll("GFFT_R2C_FUSED_DIT", 1) != 0) {
-        c2c.init(dtype, lh, batch_hint, 0);  // column pass, tables and workspace of the tile path
         rowdit = k;
         tw_rowdit = cached_table("rowdit/" + std::to_string(d) + "/" + std::to_string(k->logb), d, k->twcount,
                                  [k](void *buf) { k->fill(buf); });
+        // the persistent four-step kernel's real-input version (its row
+        // items apply the DIT), on request (GFFT_R2C_FS=1): measured on
+        // GB300 at n = 2^16 .. 2^22 (batches of 512 MB) it is 2-20 % slower
+        // than the tile launches below, which stay the default
+        int nvar = 0;
+        const FourStepKernel *const *vars = fourstep_variants(dtype, lh, &nvar);
+        bool has_dit = false;
+        for (int i = 0; i < nvar; i++) has_dit = has_dit || vars[i]->dit;
+        if (has_dit && env_ll("GFFT_R2C_FS", 0) != 0) {
+            c2c.init(dtype, lh, batch_hint, 1, true);
+            if (c2c.algo == 3 && c2c.fs_real) {
+                algo = 4;
+                return;
+            }
+            c2c.release();
+            c2c = C2CCore();
+        }
+        c2c.init(dtype, lh, batch_hint, 0);  // column pass, tables and workspace of the tile path
         algo = 3;
         return;
     }
@@ -310,7 +359,7 @@ void R2CCore::init(int dtype_, int logn_, int half_, long long batch_hint)
 int R2CCore::launches(long long batch) const
 {
     if (algo == 2) return c2c.launches(batch) + 1;
-    if (algo == 3) return c2c.launches(batch);
+    if (algo == 3 || algo == 4) return c2c.launches(batch);
     return 1;
 }
 
@@ -323,9 +372,14 @@ void R2CCore::run(const void *in, void *out, long long batch, long long idist, l
     } else if (algo == 1) {
         check_cuda(launch_r2c_fused(dtype, logn - 1, mode, in, out, batch, idist, odist, tw, dtw, st, scale),
                    "launch fused R2C");
-    } else if (algo == 3 && mode == 0) {
+    } else if (algo == 4 && mode == 0 && c2c.run_persistent(0, in, out, batch, idist / 2, odist, st, scale, dtw)) {
+        // one persistent launch: column items, then row items that apply
+        // the DIT adjustment and store the half spectrum
+    } else if ((algo == 3 || algo == 4) && mode == 0) {
         // column pass of the n/2-point split into the workspace, then the
         // row pass with the DIT adjustment fused, straight into the spectrum
+        // (also the persistent plan's path for inputs its tensor copies
+        // cannot read)
         const long long A = 1LL << c2c.logA, B = 1LL << c2c.logB, N = A * B;
         const size_t eb = cplx_bytes(dtype);
         for (long long g0 = 0; g0 < batch; g0 += c2c.group) {

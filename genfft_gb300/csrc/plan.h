@@ -25,6 +25,8 @@ struct C2CCore {
     // persistent four-step: kernel, ring of `fs_slots` transforms, counters
     const FourStepKernel *fs = nullptr;
     int fs_slots = 0, fs_lag = 0, fs_grid = 0;
+    int fs_nr = 0;            // row items per transform
+    bool fs_real = false;     // real-input mode: the kernel's DIT version
     int *fs_ctr = nullptr;
     const void *tw_a = nullptr, *tw_b = nullptr;
     int logA = 0, logB = 0, ccol = 0, crow = 0, lo_bits = 0;
@@ -35,13 +37,19 @@ struct C2CCore {
     size_t ws_bytes = 0;
 
     // path: -1 the measured default (or GFFT_FS), 1 the persistent
-    // four-step kernel, 0 the tile launches
-    void init(int dtype, int logn, long long batch_hint, int path = -1);
+    // four-step kernel, 0 the tile launches.  real_rows (with path 1): a
+    // variant with a real-input version, scheduled for its row items
+    void init(int dtype, int logn, long long batch_hint, int path = -1, bool real_rows = false);
     void release();
     int launches(long long batch) const;
     // strides in complex elements; four-step needs unit element strides
     void run(int inverse, const void *in, void *out, long long batch, long long idist, long long odist,
              long long istride, long long ostride, cudaStream_t st, double scale = 1.0) const;
+    // persistent four-step: the launches over `batch` transforms (dtw: the
+    // DIT twiddles in real-input mode); false, with nothing launched, when
+    // the input cannot be read by tensor copies (not 16-byte aligned)
+    bool run_persistent(int inverse, const void *in, void *out, long long batch, long long idist, long long odist,
+                        cudaStream_t st, double scale, const void *dtw = nullptr) const;
     // persistent four-step only: one launch whose row tiles wait on column
     // tiles that are never scheduled (the bounded wait must run out)
     void run_stalled(const void *in, void *out, cudaStream_t st) const;
@@ -77,7 +85,8 @@ cudaError_t launch_rowpass_dit(const RowDitKernel &k, const void *in, void *out,
 struct R2CCore {
     int dtype = 0, logn = 0, half = 1;
     // 0 n == 1, 1 fused, 2 C2C(n/2) + DIT pass, 3 four-step column pass +
-    // row pass with the DIT fused (half spectrum; other modes as 2)
+    // row pass with the DIT fused, 4 one persistent four-step launch whose
+    // row items apply the DIT (3 and 4: half spectrum; other modes as 2)
     int algo = 0;
     const void *tw = nullptr, *dtw = nullptr;
     const RowDitKernel *rowdit = nullptr;

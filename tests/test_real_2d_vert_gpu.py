@@ -285,3 +285,71 @@ def test_real_fft_fused_dit_row_pass(gfft, logn):
         assert np.all(np.isfinite(got.view(np.float32)))  # every bin written
         assert np.linalg.norm(got - ref) / np.linalg.norm(ref) <= bound(np.float32, n)
     assert np.linalg.norm(outs[0] - outs[1]) / np.linalg.norm(ref) <= 1e-6
+
+
+def _plan_with_env(gfft, env, *args):
+    import os
+    old = {k: os.environ.get(k) for k in env}
+    os.environ.update(env)
+    try:
+        return gfft.Plan(*args)
+    finally:
+        for k, v in old.items():
+            if v is None:
+                os.environ.pop(k)
+            else:
+                os.environ[k] = v
+
+
+@pytest.mark.parametrize("logn,cc", [(16, 0), (17, 0), (17, 32), (18, 0), (18, 32), (19, 0), (19, 16), (20, 0),
+                                     (20, 8), (21, 0), (21, 4)])
+def test_real_fft_persistent_dit(gfft, logn, cc):
+    """Half-spectrum R2C through one persistent four-step launch whose row
+    items apply the DIT adjustment (rows paired with their mirrors, row 0
+    alone), for several tile shapes, over batches that cycle the workspace
+    ring more than once: against FP64 and bit-for-bit close to the
+    separate-pass path."""
+    import torch
+    n = 1 << logn
+    batch = max(3, (48 << 20) // (4 * n))
+    g = torch.Generator(device="cuda").manual_seed(100 + logn)
+    x = torch.rand(batch, n, dtype=torch.float32, device="cuda", generator=g) * 2 - 1
+    env = {"GFFT_R2C_FS": "1", "GFFT_FS_CC": str(cc)}
+    p = _plan_with_env(gfft, env, gfft.KIND_R2C, gfft.F32, n, 0, batch, gfft.FLAG_HALF_SPECTRUM)
+    assert p.launches() == 1
+    y = torch.full((batch, n // 2 + 1), float("nan"), dtype=torch.complex64, device="cuda")
+    p.exec(y, x)
+    torch.cuda.synchronize()
+    got = host(y)
+    ref = np.fft.rfft(x.cpu().numpy().astype(np.float64))
+    assert np.all(np.isfinite(got.view(np.float32)))  # every bin written
+    err = np.linalg.norm(got - ref, axis=1) / np.linalg.norm(ref, axis=1)
+    assert err.max() <= bound(np.float32, n)
+    q = _plan_with_env(gfft, {"GFFT_R2C_FUSED_DIT": "0", "GFFT_R2C_FS": "0"}, gfft.KIND_R2C, gfft.F32, n, 0,
+                       batch, gfft.FLAG_HALF_SPECTRUM)
+    y2 = torch.empty_like(y)
+    q.exec(y2, x)
+    assert np.linalg.norm(got - host(y2)) / np.linalg.norm(ref) <= 1e-6
+    # norm scaling applied in the row items
+    y3 = torch.empty_like(y)
+    p.exec(y3, x, scale=0.25)
+    assert np.array_equal(host(y3), got * np.float32(0.25))
+
+
+def test_real_fft_persistent_dit_unaligned_input(gfft):
+    """An input the tensor copies cannot read (8-byte offset) takes the tile
+    column pass with the fused-DIT row pass: same spectrum."""
+    import torch
+    n = 1 << 18
+    batch = 4
+    g = torch.Generator(device="cuda").manual_seed(7)
+    buf = torch.rand(batch * n + 2, dtype=torch.float32, device="cuda", generator=g)
+    x = buf[2:].view(batch, n)
+    assert x.data_ptr() % 16 == 8
+    p = _plan_with_env(gfft, {"GFFT_R2C_FS": "1"}, gfft.KIND_R2C, gfft.F32, n, 0, batch, gfft.FLAG_HALF_SPECTRUM)
+    y = torch.full((batch, n // 2 + 1), float("nan"), dtype=torch.complex64, device="cuda")
+    p.exec(y, x)
+    torch.cuda.synchronize()
+    ref = np.fft.rfft(x.cpu().numpy().astype(np.float64))
+    got = host(y)
+    assert np.linalg.norm(got - ref) / np.linalg.norm(ref) <= bound(np.float32, n)
