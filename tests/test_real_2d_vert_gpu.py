@@ -353,3 +353,23 @@ def test_real_fft_persistent_dit_unaligned_input(gfft):
     ref = np.fft.rfft(x.cpu().numpy().astype(np.float64))
     got = host(y)
     assert np.linalg.norm(got - ref) / np.linalg.norm(ref) <= bound(np.float32, n)
+
+
+def test_real_fft_full_size_2_20_x64(gfft):
+    """The R2C benchmark size (n = 2^20, batch 64): Parseval on every row
+    (real input: |X_0|^2 + |X_{n/2}|^2 + 2 sum |X_k|^2 = n sum x^2) and the
+    first and last rows against an FP64 transform."""
+    import torch
+    n, batch = 1 << 20, 64
+    g = torch.Generator(device="cuda").manual_seed(20)
+    x = torch.rand(batch, n, dtype=torch.float32, device="cuda", generator=g) * 2 - 1
+    y = gfft.rfft(x, half=True)
+    assert y.shape == (batch, n // 2 + 1)
+    p = y.to(torch.complex128).abs() ** 2
+    lhs = p[:, 0] + p[:, -1] + 2 * p[:, 1:-1].sum(dim=1)
+    rhs = n * (x.double() ** 2).sum(dim=1)
+    assert torch.max(torch.abs(lhs / rhs - 1)).item() <= 1e-5
+    for b in (0, batch - 1):
+        ref = np.fft.rfft(x[b].cpu().numpy().astype(np.float64))
+        got = host(y[b])
+        assert np.linalg.norm(got - ref) / np.linalg.norm(ref) <= bound(np.float32, n)
