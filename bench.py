@@ -259,12 +259,17 @@ def time_cpu(kind, dtype, n0, n1, batch, budget_s=8.0, max_reps=20):
         y, z = np.empty_like(x), np.empty_like(x)
         fn = getattr(L, f"{prefix}fft_batch_{s}")
         run = lambda: (fn(p(y), p(x), n0, batch, 0, cores), fn(p(z), p(y), n0, batch, 1, cores))  # noqa: E731
+        # one thread over 1/cores of the batch: about one step's time
+        sub = max(1, batch // cores)
+        run1 = lambda: (fn(p(y), p(x), n0, sub, 0, 1), fn(p(z), p(y), n0, sub, 1, 1))  # noqa: E731
         desc, threads = f"forward+inverse of the full {batch} x {n0} batch", cores
     elif kind == "r2c":
         x = rng.uniform(-1, 1, (batch, n0)).astype(rdt)
         y = np.empty((batch, n0), dtype=cdt)
         fn = getattr(L, f"{prefix}real_fft_batch_f")
         run = lambda: fn(p(y), n0, p(x), n0, n0, batch, 1, cores)  # noqa: E731
+        sub = max(1, batch // cores)
+        run1 = lambda: fn(p(y), n0, p(x), n0, n0, sub, 1, 1)  # noqa: E731
         desc, threads = f"half-spectrum forward of the full {batch} x {n0} batch", cores
     elif kind == "c2d":
         x = (rng.uniform(-1, 1, (n1, n0)) + 1j * rng.uniform(-1, 1, (n1, n0))).astype(cdt)
@@ -288,8 +293,21 @@ def time_cpu(kind, dtype, n0, n1, batch, budget_s=8.0, max_reps=20):
     nb = batch if kind in ("c2c", "r2c") else 1
     step_bytes = execs_per_step(kind) * nb * algo_bytes_per_transform(kind, dtype, n0, n1)
     med = statistics.median(times)
-    return {"value": step_bytes / med / 1e9, "unit": "GB/s", "cores": threads, "kind": kindname,
-            "sample": f"{len(times)} steps ({desc}), {threads} threads, median step {med * 1e3:.1f} ms"}, med, len(times)
+    out = {"value": step_bytes / med / 1e9, "unit": "GB/s", "cores": threads, "kind": kindname,
+           "sample": f"{len(times)} steps ({desc}), {threads} threads, median step {med * 1e3:.1f} ms"}
+    if kind in ("c2c", "r2c") and threads > 1:
+        # the same algorithm on one core, for the per-core figure
+        run1()
+        t1 = []
+        t_start = time.perf_counter()
+        while len(t1) < max_reps and (time.perf_counter() - t_start) < budget_s / 2:
+            t0 = time.perf_counter()
+            run1()
+            t1.append(time.perf_counter() - t0)
+        med1 = statistics.median(t1)
+        out["value_1thread"] = execs_per_step(kind) * sub * algo_bytes_per_transform(kind, dtype, n0, n1) / med1 / 1e9
+        out["sample_1thread"] = f"{len(t1)} steps over {sub} of the {batch} transforms, 1 thread, median {med1 * 1e3:.1f} ms"
+    return out, med, len(times)
 
 
 # ---------------------------------------------------------------------------
