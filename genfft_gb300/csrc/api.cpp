@@ -255,8 +255,8 @@ static bool overlaps(const void *a, size_t an, const void *b, size_t bn)
 
 // `scale` multiplies every output (norm= scaling), applied by the kernel
 // that writes the result
-static void exec_plan(gfft_plan_s &p, int inverse, void *out, const void *in, const Layout &L, cudaStream_t st,
-                      double scale = 1.0)
+static void exec_body(gfft_plan_s &p, int inverse, void *out, const void *in, const Layout &L, cudaStream_t st,
+                      double scale)
 {
     const gfft_desc &d = p.d;
     const size_t cb = cplx_bytes(d.dtype), rb = real_bytes(d.dtype);
@@ -337,6 +337,38 @@ static void exec_plan(gfft_plan_s &p, int inverse, void *out, const void *in, co
     default:
         fail(GFFT_ERR_INVALID_PLAN, "plan has no transform kind");
     }
+}
+
+// A plan's workspace (multi-pass sizes) serves one transform at a time.
+// The reference-shaped entry points share one plan per size (as the
+// reference shares its per-size singletons, FFTLevel.h:76-88) whose
+// workspace the caller never sees, so their execs may come from several
+// threads and streams at once.  Those plans carry an event (ws_last): each
+// exec waits on its stream for the previous one's event, under a host lock,
+// and records its own, so they run in issue order.  Inside a stream capture
+// the caller orders the graph's replays; the capture records no wait.
+// Plans from gfft_plan_create carry no event: their execs are ordered by
+// the caller (one stream, or one plan per stream).
+static void exec_plan(gfft_plan_s &p, int inverse, void *out, const void *in, const Layout &L, cudaStream_t st,
+                      double scale = 1.0)
+{
+    if (!p.ws_last) {
+        exec_body(p, inverse, out, in, L, st, scale);
+        return;
+    }
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess) {
+        (void)cudaGetLastError();
+        cs = cudaStreamCaptureStatusActive;
+    }
+    if (cs != cudaStreamCaptureStatusNone) {
+        exec_body(p, inverse, out, in, L, st, scale);
+        return;
+    }
+    std::lock_guard<std::mutex> lk(p.ws_mu);
+    check_cuda(cudaStreamWaitEvent(st, p.ws_last, 0), "workspace order wait");
+    exec_body(p, inverse, out, in, L, st, scale);
+    check_cuda(cudaEventRecord(p.ws_last, st), "workspace order record");
 }
 
 // Adjoint of the plan's transform in direction `inverse` (reverse-mode
@@ -457,6 +489,7 @@ static void destroy_plan(gfft_plan_s *p)
         if (p->ev_done[i]) cudaEventDestroy(p->ev_done[i]);
     }
     if (p->compute_stream) cudaStreamDestroy(p->compute_stream);
+    if (p->ws_last) cudaEventDestroy(p->ws_last);
     p->c2c.release();
     p->r2c.release();
     p->c2r.release();
@@ -489,6 +522,13 @@ static gfft_plan_s *cached_plan(int kind, int dtype, long long n0, long long n1,
     d.n1 = n1;
     d.batch = 1 << 20;  // sizes the workspace for full groups; the batch is per call
     gfft_plan_s *p = make_plan(d);
+    if (p->workspace_bytes() > 0) {
+        cudaError_t e = cudaEventCreateWithFlags(&p->ws_last, cudaEventDisableTiming);
+        if (e != cudaSuccess) {
+            destroy_plan(p);
+            check_cuda(e, "cudaEventCreate");
+        }
+    }
     cache.emplace(key, p);
     return p;
 }
@@ -586,7 +626,7 @@ gfft_status gfft_plan_workspace_size(gfft_plan plan, size_t *bytes)
     GFFT_GUARD({
         if (!bytes) fail(GFFT_ERR_INVALID_VALUE, "NULL argument");
         gfft_plan_s *p = checked(plan);
-        *bytes = p->c2c.ws_bytes + p->r2c.c2c.ws_bytes + p->tc.ws_bytes;
+        *bytes = p->workspace_bytes();
     });
 }
 

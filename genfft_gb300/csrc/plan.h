@@ -191,4 +191,9 @@ struct gfft_plan_s {
     cudaStream_t host_streams[3] = {nullptr, nullptr, nullptr};  // copies
     cudaStream_t compute_stream = nullptr;                        // transforms, in order
     cudaEvent_t ev_in[3] = {nullptr, nullptr, nullptr}, ev_done[3] = {nullptr, nullptr, nullptr};
+    // execs that use the workspace are ordered on the GPU in issue order,
+    // whatever their streams: each waits for the last one's event
+    std::mutex ws_mu;
+    cudaEvent_t ws_last = nullptr;
+    size_t workspace_bytes() const { return c2c.ws_bytes + r2c.c2c.ws_bytes + c2r.c2c.ws_bytes + tc.ws_bytes; }
 };

@@ -126,7 +126,11 @@ gfft_status gfft_plan_workspace_size(gfft_plan plan, size_t *bytes);
 /* ---- reference-shaped entry points (device pointers) ------------------ */
 /* Each mirrors one call of the reference C++ API; plans are cached per
  * (kind, type, size) like the reference's per-size singletons
- * (FFTLevel.h:76-88), but creation here is mutex-guarded. */
+ * (FFTLevel.h:76-88), but creation here is mutex-guarded.  Like the
+ * reference's transforms, these calls may be made from any thread on any
+ * stream at once: where the cached plan has a workspace (multi-pass
+ * sizes), its transforms run one after another on the GPU, in issue order,
+ * whatever their streams. */
 
 /* FFT<T>(n).transform<inverse>(out, in) over `batch` dense transforms
  * (fft.h:80-85).  out != in is not required here (in-place is allowed). */

@@ -111,3 +111,41 @@ def test_multipass_strided_batches(gfft, oracle):
     assert oracle.rel_rms(got, exact) <= bound(np.complex64, n)
     assert np.all(tout.cpu().numpy()[:, n:] == 0)
     assert p.launches() == 1  # one persistent four-step launch (fp32, n = 2^16 .. 2^19)
+
+
+@pytest.mark.parametrize("logn", [17, 20])
+def test_reference_shaped_calls_from_two_threads(gfft, logn):
+    """gfft_fft_transform (FFT<float>(n).transform) from two host threads on
+    two streams at once.  The per-size plan behind it has one workspace
+    (persistent ring at 2^17, tile workspace at 2^20); its transforms must
+    run one after another, so every result equals the one-stream result."""
+    import threading
+    import torch
+    n, batch, reps = 1 << logn, 6, 12
+    g = torch.Generator(device="cuda").manual_seed(logn)
+    xs = [torch.randn(batch, n, dtype=torch.complex64, device="cuda", generator=g) for _ in range(2)]
+    refs = [gfft.fft(x) for x in xs]
+    torch.cuda.synchronize()
+    outs = [[torch.empty_like(xs[0]) for _ in range(reps)] for _ in range(2)]
+    errors = []
+
+    def worker(i):
+        try:
+            s = torch.cuda.Stream()
+            with torch.cuda.stream(s):
+                for r in range(reps):
+                    gfft._check(gfft.lib().gfft_fft_transform(gfft.F32, n, batch, 0, outs[i][r].data_ptr(),
+                                                              xs[i].data_ptr(), s.cuda_stream))
+            s.synchronize()
+        except Exception as e:  # reported by the main thread
+            errors.append(e)
+
+    th = [threading.Thread(target=worker, args=(i,)) for i in range(2)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    assert not errors, errors
+    for i in range(2):
+        for r in range(reps):
+            assert torch.equal(outs[i][r], refs[i]), (i, r)
