@@ -71,6 +71,12 @@ THROTTLE_BITS = {
 }
 
 
+def metric_name(kind, dtype):
+    """The metric both arms report for a workload (GB/s of algorithmic
+    bytes: one read of the input and one write of the output per exec)."""
+    return f"{'ragged c2c' if kind == 'ragged' else kind} {dtype} GB/s (algorithmic, HBM-resident)"
+
+
 def log(*a):
     print(*a, file=sys.stderr, flush=True)
 
@@ -104,7 +110,7 @@ def flops_per_transform(kind, n0, n1):
 def execs_per_step(kind):
     """forward + unscaled inverse for complex kinds; forward only for real
     input (the reference has no real inverse, FFTReal.h:127-130)."""
-    return 2 if kind in ("c2c", "c2d") else 1
+    return 2 if kind in ("c2c", "c2d", "ragged") else 1
 
 
 def measured_peak():
@@ -254,7 +260,26 @@ def time_cpu(kind, dtype, n0, n1, batch, budget_s=8.0, max_reps=20):
     rdt = np.float32 if dtype == "f32" else np.float64
     p = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
     s = dtype[0]
-    if kind == "c2c":
+    if kind == "ragged":
+        # the reference has no ragged call: it transforms each size class
+        # as one batch (favouring the CPU), over the first 1000 of the
+        # transforms (same size law)
+        sizes = ragged_sizes(batch)[:1000]
+        classes = sorted(set(sizes))
+        bufs = {n: (rng.standard_normal((sizes.count(n), n)) + 1j * rng.standard_normal((sizes.count(n), n))).astype(
+            np.complex64) for n in classes}
+        outs = {n: np.empty_like(b) for n, b in bufs.items()}
+        outs2 = {n: np.empty_like(b) for n, b in bufs.items()}
+        fn = getattr(L, f"{prefix}fft_batch_f")
+
+        def run():
+            for n in classes:
+                c = bufs[n].shape[0]
+                fn(p(outs[n]), p(bufs[n]), n, c, 0, cores)
+                fn(p(outs2[n]), p(outs[n]), n, c, 1, cores)
+        ragged_bytes = 2 * sum(16 * n for n in sizes)
+        desc, threads = f"forward+inverse of the first {len(sizes)} transforms, one batch per size class", cores
+    elif kind == "c2c":
         x = (rng.standard_normal((batch, n0)) + 1j * rng.standard_normal((batch, n0))).astype(cdt)
         y, z = np.empty_like(x), np.empty_like(x)
         fn = getattr(L, f"{prefix}fft_batch_{s}")
@@ -291,7 +316,10 @@ def time_cpu(kind, dtype, n0, n1, batch, budget_s=8.0, max_reps=20):
         run()
         times.append(time.perf_counter() - t0)
     nb = batch if kind in ("c2c", "r2c") else 1
-    step_bytes = execs_per_step(kind) * nb * algo_bytes_per_transform(kind, dtype, n0, n1)
+    if kind == "ragged":
+        step_bytes = ragged_bytes
+    else:
+        step_bytes = execs_per_step(kind) * nb * algo_bytes_per_transform(kind, dtype, n0, n1)
     med = statistics.median(times)
     out = {"value": step_bytes / med / 1e9, "unit": "GB/s", "cores": threads, "kind": kindname,
            "sample": f"{len(times)} steps ({desc}), {threads} threads, median step {med * 1e3:.1f} ms"}
@@ -351,7 +379,7 @@ def run_reference(args):
     cb, med, reps = time_cpu(kind, dtype, n0, n1, batch, budget_s=max(5.0, min(60.0, 3.0 * steps)),
                              max_reps=steps)
     line = {
-        "impl": "reference", "metric": f"{kind} {dtype} GB/s", "value": round(cb["value"], 3),
+        "impl": "reference", "metric": metric_name(kind, dtype), "value": round(cb["value"], 3),
         "unit": "GB/s", "n_gpus": args.gpus, "steps": reps, "warmup": 1,
         "ms_per_step": round(med * 1e3, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": dtype, "data": "synthetic",
@@ -516,7 +544,7 @@ def run_ragged(args):
         errs.append(float(np.linalg.norm(ys[o:o + n] - ref) / np.linalg.norm(ref)))
     if rank == 0:
         line = {
-            "metric": "ragged c2c f32 GB/s (algorithmic, HBM-resident)", "value": round(gbs, 2), "unit": "GB/s",
+            "metric": metric_name("ragged", "f32"), "value": round(gbs, 2), "unit": "GB/s",
             "n_gpus": world, "steps": K, "warmup": max(3, args.warmup), "ms_per_step": round(ms / K, 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": args.workload, "transforms": len(sizes), "sizes": "2^k, k ~ U{6..18}, seed 20240",
@@ -537,6 +565,9 @@ def run_ragged(args):
                     "steps": e2e_steps},
             "gpu_launches": 2 * K, "check": max(errs), "clocks": clk.summary(),
         }
+        if not args.no_cpu and world == 1:
+            cb, _, _ = time_cpu("ragged", "f32", 0, 0, len(sizes), budget_s=args.cpu_budget, max_reps=5)
+            line["cpu_baseline"] = cb
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
@@ -670,7 +701,7 @@ def run_ours(args):
         del plain, pp
     if rank == 0:
         line = {
-            "metric": f"{kind} {dtype} GB/s (algorithmic, HBM-resident)"
+            "metric": metric_name(kind, dtype)
                       + (f", {MODE_NAMES[mode]} tensor-core path" if mode else ""),
             "value": round(gbs, 2), "unit": "GB/s", "n_gpus": world, "steps": K,
             "warmup": max(3, args.warmup), "ms_per_step": round(ms / K, 4),
@@ -699,7 +730,7 @@ def run_ours(args):
             "check": check, "e2e_check": e2e_check, "accuracy": accuracy,
             "clocks": clk.summary(),
         }
-        if not args.no_cpu:
+        if not args.no_cpu and world == 1:
             cb, _, _ = time_cpu(kind, dtype, n0, n1, batch, budget_s=args.cpu_budget, max_reps=5)
             line["cpu_baseline"] = cb
         print(json.dumps(line), flush=True)
