@@ -394,12 +394,23 @@ def run_reference(args):
     return 0
 
 
-def kernel_name(G, kind, dtype, n0, mode=0):
-    """The dominant kernel of one exec of the workload."""
+def kernel_name(G, kind, dtype, n0, mode=0, launches=1):
+    """The kernels of one exec of the workload (`launches`: the plan's
+    launch count for the batch; the four-step path is one persistent
+    launch, or column + row tile launches per workspace group)."""
     if mode:
         return "k_tc"
+    fused = n0 <= G.max_fused_size(G.F32 if dtype == "f32" else G.F64)
     if kind == "c2c":
-        return "k_c2c_fused" if n0 <= G.max_fused_size(G.F32 if dtype == "f32" else G.F64) else "k_fourstep"
+        if fused:
+            return "k_c2c_fused"
+        return "k_fourstep" if launches == 1 else "k_colpass_tma + k_rowpass_tma"
+    if kind == "r2c":
+        return "k_r2c_fused" if n0 // 2 <= G.max_fused_size(G.F32) else "k_colpass_tma + k_rowpass_dit"
+    if kind == "c2d":
+        return "k_c2c_fused (rows) + k_colpass (columns)"
+    if kind == "r2d":
+        return "k_r2c_fused (rows) + k_colpass Hermitian (columns)"
     return "plan kernels"
 
 
@@ -557,7 +568,9 @@ def run_ragged(args):
             "autotune": {"lag_factor": tune[0], "ctas_per_sm": tune[1], "large_first": tune[2]},
             "roofline": {"bound": "hbm", "achieved": round(bytes_exec / (exec_ms / 1e3) / 1e9, 1), "peak": peak,
                          "unit": "GB/s", "frac": round(bytes_exec / (exec_ms / 1e3) / 1e9 / peak, 4),
-                         "traffic": traffic_from_profile(args.workload), "peak_source": peak_src,
+                         "traffic": traffic_from_profile(args.workload),
+                         "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)" if peak_src == "measured"
+                         else "fallback 6800 GB/s",
                          "kernel": "k_ragged", "launches_per_exec": 1, "avg_exec_ms": round(exec_ms, 5),
                          "algorithmic_bytes_per_exec": bytes_exec},
             "e2e": {"value": round(e2e_gbs, 2), "unit": "GB/s", "h2d_bytes_per_step": 2 * 8 * plan.elements,
@@ -719,7 +732,7 @@ def run_ours(args):
                          "frac": round(achieved / peak, 4), "traffic": traffic,
                          "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)" if peak_src == "measured"
                          else "fallback 6800 GB/s",
-                         "kernel": kernel_name(G, kind, dtype, n0, mode),
+                         "kernel": kernel_name(G, kind, dtype, n0, mode, launches_per_exec),
                          "launches_per_exec": launches_per_exec, "avg_exec_ms": round(avg_exec_ms, 5),
                          "avg_launch_ms": round(avg_launch_ms, 5),
                          "algorithmic_bytes_per_exec": batch * per_transform},
