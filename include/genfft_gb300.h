@@ -206,7 +206,9 @@ gfft_status gfft_fft_transform_noalloc(int dtype, int n, long long batch, int in
  * back (transform i starts at the sum of the earlier sizes).  One exec is
  * one CUDA-graph replay of a single persistent kernel; the graph is
  * captured on the first exec with a given (in, out, direction).  The plan
- * owns scratch for its transforms above 2^12 points. */
+ * owns scratch for its transforms above 2^12 points and a work counter:
+ * execs of one plan must be ordered by the caller (one stream, or events);
+ * use one plan per stream to run ragged batches concurrently. */
 typedef struct gfft_ragged_s *gfft_ragged;
 gfft_status gfft_ragged_create(gfft_ragged *plan, int dtype, const long long *sizes, long long count);
 gfft_status gfft_ragged_destroy(gfft_ragged plan);
