@@ -149,3 +149,20 @@ def test_reference_shaped_calls_from_two_threads(gfft, logn):
     for i in range(2):
         for r in range(reps):
             assert torch.equal(outs[i][r], refs[i]), (i, r)
+
+
+@pytest.mark.parametrize("dt,logn", [(np.complex64, 23), (np.complex64, 24), (np.complex128, 23)])
+def test_largest_sizes(gfft, oracle, dt, logn):
+    """The reference's largest size, 2^23 (FFT<T>::GetImpl covers 2^0 ..
+    2^23, fft_impl_generic.h:245-279), and fp32 2^24: forward and unscaled
+    inverse against an FP64 transform."""
+    import torch
+    n = 1 << logn
+    rng = np.random.default_rng(logn)
+    x = (rng.standard_normal(n) + 1j * rng.standard_normal(n)).astype(dt)[None, :]
+    t = torch.from_numpy(x).cuda()
+    for inv in (False, True):
+        got = gfft.fft(t, inv).cpu().numpy()
+        x64 = x.astype(np.complex128)
+        exact = np.fft.ifft(x64) * n if inv else np.fft.fft(x64)
+        assert oracle.rel_rms(got, exact) <= bound(dt, n), (logn, inv)
