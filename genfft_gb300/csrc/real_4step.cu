@@ -45,7 +45,7 @@ struct RowDitCfg {
 // in: the column pass's output, rows of B; out: the half spectrum, H + 1
 // bins per transform.  grid: (A / (2 CH) + 1) x batch.
 template <typename T, int LOGB, int CH, int E_>
-__global__ void __launch_bounds__(RowDitCfg<T, LOGB, CH, E_>::THREADS)
+__global__ void __launch_bounds__(RowDitCfg<T, LOGB, CH, E_>::THREADS, 2)
     k_rowpass_dit(const cpx<T> *__restrict__ in, cpx<T> *__restrict__ out, long long A, long long idist,
                   long long odist, const cpx<T> *__restrict__ tw, const cpx<T> *__restrict__ dtw, T scale)
 {

@@ -64,6 +64,25 @@ bool tma_disabled()
     return off;
 }
 
+// single-buffered TMA tile kernels: GFFT_TMA1 unset or 1 = used (row and
+// column passes), 2 = column passes only, 0 = not used
+static int tma1_mode()
+{
+    static const int m = [] {
+        const char *v = std::getenv("GFFT_TMA1");
+        return (v && *v) ? std::atoi(v) : 1;
+    }();
+    return m;
+}
+
+static bool use_tma(const TileKernel &k)
+{
+    if (!k.tma_fwd || tma_disabled()) return false;
+    if (k.tma_stages != 1) return true;
+    const int m = tma1_mode();
+    return m == 1 || (m == 2 && !k.tma_row);
+}
+
 using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
@@ -163,11 +182,11 @@ int tile_widest(int dtype, int variant, int logl, int max_c)
         if (!narrowest || c < narrowest) narrowest = c;
         if (c > max_c) continue;
         best = std::max(best, c);
-        if (kv.second.tma_fwd) best_tma = std::max(best_tma, c);
+        if (use_tma(kv.second)) best_tma = std::max(best_tma, c);
     }
     // prefer the widest tile that has a TMA-pipelined version; else the
     // widest under the cap; else the narrowest there is
-    if (best_tma && !tma_disabled()) return best_tma;
+    if (best_tma) return best_tma;
     return best ? best : narrowest;
 }
 
@@ -183,7 +202,7 @@ cudaError_t launch_colpass(const TileKernel &k, int inverse, long long tiles, lo
     // strides; in-place runs (out == in) are fine, each tile is loaded whole
     // before it is written back
     const size_t eb = (size_t)k.elem_bytes;
-    if (k.tma_fwd && !tma_disabled() && encode_fn() && aligned16(in) && (ld_in * eb) % 16 == 0 &&
+    if (use_tma(k) && encode_fn() && aligned16(in) && (ld_in * eb) % 16 == 0 &&
         (nbatch == 1 || (idist * eb) % 16 == 0) && ncols * (eb / 8) < (1LL << 32) && nbatch < (1LL << 31)) {
         const int units = (int)(eb / 8);
         CUtensorMap map;
@@ -232,7 +251,7 @@ cudaError_t launch_rowpass(const TileKernel &k, int inverse, long long tiles, lo
     float scale_f = (float)scale;
     void *scale_p = k.elem_bytes == 8 ? (void *)&scale_f : (void *)&scale;
     const size_t eb = (size_t)k.elem_bytes;
-    if (k.tma_fwd && !tma_disabled() && aligned16(in) && (ld_in * eb) % 16 == 0 &&
+    if (use_tma(k) && aligned16(in) && (ld_in * eb) % 16 == 0 &&
         (nbatch == 1 || (idist * eb) % 16 == 0)) {
         const void *fn = inverse ? k.tma_inv : k.tma_fwd;
         cudaError_t e = ensure_smem(fn, k.tma_smem);

@@ -30,11 +30,24 @@ struct TileReg {
             k.threads = Cfg::THREADS;
             k.smem = Cfg::SMEM;
             using TCfg = RowTmaCfg<T, LOGL, C, E>;
+            using TCfg1 = RowTmaCfg<T, LOGL, C, E, 1>;
             if constexpr (TCfg::SMEM <= 220 * 1024 && SP::N * sizeof(cpx<T>) % 16 == 0) {
                 k.tma_fwd = (const void *)&k_rowpass_tma<T, LOGL, C, E, false>;
                 k.tma_inv = (const void *)&k_rowpass_tma<T, LOGL, C, E, true>;
                 k.tma_threads = TCfg::THREADS;
                 k.tma_smem = TCfg::SMEM;
+                k.tma_stages = 2;
+            } else if constexpr (LOGL >= 12 && TCfg1::SMEM <= 220 * 1024 && SP::N * sizeof(cpx<T>) % 16 == 0) {
+                // single-buffered rows only where the double-buffered tile
+                // is two rows (16-byte store runs): measured on GB300 at
+                // n = 2^23 / 2^24 +18 % / +19 %; against four- or eight-row
+                // double-buffered tiles (n = 2^20 .. 2^22) it is slower
+                k.tma_fwd = (const void *)&k_rowpass_tma<T, LOGL, C, E, false, 1>;
+                k.tma_inv = (const void *)&k_rowpass_tma<T, LOGL, C, E, true, 1>;
+                k.tma_threads = TCfg1::THREADS;
+                k.tma_smem = TCfg1::SMEM;
+                k.tma_stages = 1;
+                k.tma_row = true;
             }
         } else {
             using Cfg = ColCfg<T, LOGL, C, E>;
@@ -44,6 +57,7 @@ struct TileReg {
             k.threads = Cfg::THREADS;
             k.smem = Cfg::SMEM;
             using TCfg = ColTmaCfg<T, LOGL, C, E>;
+            using TCfg1 = ColTmaCfg<T, LOGL, C, E, 1>;
             if constexpr (!br && TCfg::SMEM <= 220 * 1024 && C * sizeof(cpx<T>) % 16 == 0) {
                 k.tma_fwd = (const void *)&k_colpass_tma<T, LOGL, C, E, false, tw4, herm>;
                 k.tma_inv = (const void *)&k_colpass_tma<T, LOGL, C, E, true, tw4, herm>;
@@ -52,6 +66,19 @@ struct TileReg {
                 k.tma_boxr = TCfg::BOXR;
                 k.tma_rows = TCfg::N;
                 k.tma_c = C;
+                k.tma_stages = 2;
+            } else if constexpr (tw4 && TCfg1::SMEM <= 220 * 1024 && C * sizeof(cpx<T>) % 16 == 0) {
+                // four-step column pass only: measured on GB300, the wider
+                // single-buffered tile beats the narrower double-buffered one
+                // (n = 2^20 .. 2^24: 7-42 %); for 2D columns it does not
+                k.tma_fwd = (const void *)&k_colpass_tma<T, LOGL, C, E, false, tw4, herm, 1>;
+                k.tma_inv = (const void *)&k_colpass_tma<T, LOGL, C, E, true, tw4, herm, 1>;
+                k.tma_threads = TCfg1::THREADS;
+                k.tma_smem = TCfg1::SMEM;
+                k.tma_boxr = TCfg1::BOXR;
+                k.tma_rows = TCfg1::N;
+                k.tma_c = C;
+                k.tma_stages = 1;
             }
         }
         k.twcount = (size_t)SP::TW;

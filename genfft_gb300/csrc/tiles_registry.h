@@ -33,6 +33,8 @@ struct TileKernel {
     int tma_boxr = 0;  // column pass: rows per tensor box
     int tma_rows = 0;  // column pass: column length (tensor rows)
     int tma_c = 0;     // columns per tile
+    int tma_stages = 0;  // 2 double-buffered, 1 single buffer
+    bool tma_row = false;  // a row-pass kernel (for the GFFT_TMA1 knob)
 };
 
 // register / look up (returns nullptr when not instantiated)

@@ -33,7 +33,9 @@ struct StageRound {
 // ---------------------------------------------------------------------------
 // row pass: C rows of L points, stored transposed (see k_rowpass)
 
-template <typename T, int LOGL, int C, int E_>
+// NSTG as for the column pass below (1: the next tile's copies start once
+// the transposed tile has been read back into registers, before the stores)
+template <typename T, int LOGL, int C, int E_, int NSTG = 2>
 struct RowTmaCfg {
     using SP = StockhamPlan<T, LOGL, E_>;
     static constexpr int N = SP::N;
@@ -42,21 +44,22 @@ struct RowTmaCfg {
     static constexpr int XPOSE = spad_size<T>(N * C);
     static constexpr int STAGE =
         StageRound<T, cmax<cmax<ROW * C, XPOSE>::value, N * C>::value>::value;  // elements
-    static constexpr size_t SMEM = 2 * (size_t)STAGE * sizeof(cpx<T>) + 64;
+    static constexpr size_t SMEM = NSTG * (size_t)STAGE * sizeof(cpx<T>) + 64;
 };
 
-template <typename T, int LOGL, int C, int E_, bool INV>
-__global__ void __launch_bounds__(RowTmaCfg<T, LOGL, C, E_>::THREADS, 1)
+template <typename T, int LOGL, int C, int E_, bool INV, int NSTG = 2>
+__global__ void __launch_bounds__(RowTmaCfg<T, LOGL, C, E_, NSTG>::THREADS, 1)
     k_rowpass_tma(const cpx<T> *__restrict__ in, cpx<T> *__restrict__ out, long long nrows, long long ld_in,
                   long long ostride, long long idist, long long odist, long long nbatch,
                   const cpx<T> *__restrict__ tw, unsigned *err, T scale)
 {
-    using Cfg = RowTmaCfg<T, LOGL, C, E_>;
+    static_assert(NSTG == 1 || NSTG == 2, "one or two stages");
+    using Cfg = RowTmaCfg<T, LOGL, C, E_, NSTG>;
     using SP = typename Cfg::SP;
     constexpr int E = SP::E, G = SP::G, N = SP::N;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     cpx<T> *const stage0 = reinterpret_cast<cpx<T> *>(smem_raw);
-    uint64_t *const bars = reinterpret_cast<uint64_t *>(smem_raw + 2 * (size_t)Cfg::STAGE * sizeof(cpx<T>));
+    uint64_t *const bars = reinterpret_cast<uint64_t *>(smem_raw + NSTG * (size_t)Cfg::STAGE * sizeof(cpx<T>));
 
     const int s = threadIdx.x / G;
     const int t = threadIdx.x - s * G;
@@ -64,8 +67,7 @@ __global__ void __launch_bounds__(RowTmaCfg<T, LOGL, C, E_>::THREADS, 1)
     const long long total = tiles * nbatch;
 
     if (threadIdx.x == 0) {
-        mbar_init(&bars[0], 1);
-        mbar_init(&bars[1], 1);
+        for (int i = 0; i < NSTG; i++) mbar_init(&bars[i], 1);
         fence_barrier_init();
     }
     __syncthreads();
@@ -82,8 +84,8 @@ __global__ void __launch_bounds__(RowTmaCfg<T, LOGL, C, E_>::THREADS, 1)
     long long w = blockIdx.x;
     if (threadIdx.x == 0 && w < total) issue(w, 0);
     for (int k = 0; w < total; w += gridDim.x, k++) {
-        const int cur = k & 1;
-        const uint32_t par = (uint32_t)((k >> 1) & 1);
+        const int cur = NSTG == 2 ? (k & 1) : 0;
+        const uint32_t par = (uint32_t)(NSTG == 2 ? ((k >> 1) & 1) : (k & 1));
         const bool ok = mbar_wait(&bars[cur], par);
         if (!__syncthreads_and(ok)) {
             if (threadIdx.x == 0) {
@@ -93,7 +95,7 @@ __global__ void __launch_bounds__(RowTmaCfg<T, LOGL, C, E_>::THREADS, 1)
             return;
         }
         // the other buffer is free (every thread finished the previous tile)
-        if (threadIdx.x == 0 && w + gridDim.x < total) {
+        if (NSTG == 2 && threadIdx.x == 0 && w + gridDim.x < total) {
             fence_proxy_async_smem();
             issue(w + gridDim.x, cur ^ 1);
         }
@@ -112,12 +114,33 @@ __global__ void __launch_bounds__(RowTmaCfg<T, LOGL, C, E_>::THREADS, 1)
         for (int q = 0; q < E; q++) S[spad<T>((t + q * G) * C + s)] = v[q];
         __syncthreads();
         cpx<T> *dst = out + b * odist + row0;
+        if constexpr (NSTG == 1) {
+            // read the transposed tile back, free the buffer for the next
+            // tile's copies, then store
+            cpx<T> o[E];
 #pragma unroll
-        for (int m = 0; m < E; m++) {
-            const int idx = threadIdx.x + m * Cfg::THREADS;
-            const int s2 = idx % C;
-            const int kk = idx / C;
-            if (kk < N && row0 + s2 < nrows) stcs_c(dst + s2 + (long long)kk * ostride, scl(S[spad<T>(idx)], scale));
+            for (int m = 0; m < E; m++) o[m] = S[spad<T>(threadIdx.x + m * Cfg::THREADS)];
+            __syncthreads();
+            if (threadIdx.x == 0 && w + gridDim.x < total) {
+                fence_proxy_async_smem();
+                issue(w + gridDim.x, 0);
+            }
+#pragma unroll
+            for (int m = 0; m < E; m++) {
+                const int idx = threadIdx.x + m * Cfg::THREADS;
+                const int s2 = idx % C;
+                const int kk = idx / C;
+                if (kk < N && row0 + s2 < nrows) stcs_c(dst + s2 + (long long)kk * ostride, scl(o[m], scale));
+            }
+        } else {
+#pragma unroll
+            for (int m = 0; m < E; m++) {
+                const int idx = threadIdx.x + m * Cfg::THREADS;
+                const int s2 = idx % C;
+                const int kk = idx / C;
+                if (kk < N && row0 + s2 < nrows)
+                    stcs_c(dst + s2 + (long long)kk * ostride, scl(S[spad<T>(idx)], scale));
+            }
         }
     }
 }
@@ -127,7 +150,12 @@ __global__ void __launch_bounds__(RowTmaCfg<T, LOGL, C, E_>::THREADS, 1)
 // the input as [batch][rows][ncols] elements of `unit` bytes (8 for fp32
 // complex; fp64 complex is two 8-byte units)
 
-template <typename T, int LOGL, int C, int E_>
+// NSTG = 2: double-buffered (the next tile lands while this one is
+// transformed).  NSTG = 1, for tiles whose two buffers do not fit: the
+// next tile's copy starts once every thread has read its last exchange
+// values, so it overlaps the twiddle and the stores of this tile, and the
+// loads cost no load instructions either way.
+template <typename T, int LOGL, int C, int E_, int NSTG = 2>
 struct ColTmaCfg {
     using SP = StockhamPlan<T, LOGL, E_>;
     static constexpr int N = SP::N;
@@ -135,23 +163,24 @@ struct ColTmaCfg {
     static constexpr int PITCH = tile_pitch<T>(N, C);
     static constexpr int BOXR = N < 256 ? N : 256;  // rows per tensor box
     static constexpr int STAGE = StageRound<T, cmax<PITCH * C, N * C>::value>::value;
-    static constexpr size_t SMEM = 2 * (size_t)STAGE * sizeof(cpx<T>) + 64;
+    static constexpr size_t SMEM = NSTG * (size_t)STAGE * sizeof(cpx<T>) + 64;
 };
 
-template <typename T, int LOGL, int C, int E_, bool INV, bool TW4, bool HERM>
-__global__ void __launch_bounds__(ColTmaCfg<T, LOGL, C, E_>::THREADS, 1)
+template <typename T, int LOGL, int C, int E_, bool INV, bool TW4, bool HERM, int NSTG = 2>
+__global__ void __launch_bounds__(ColTmaCfg<T, LOGL, C, E_, NSTG>::THREADS, 1)
     k_colpass_tma(const __grid_constant__ CUtensorMap map, cpx<T> *__restrict__ out, long long ncols,
                   long long ld_out, long long odist, long long nbatch, const cpx<T> *__restrict__ tw,
                   const cpx<T> *__restrict__ tw_lo, const cpx<T> *__restrict__ tw_hi, int lo_bits, unsigned nmask,
                   unsigned *err, T scale)
 {
-    using Cfg = ColTmaCfg<T, LOGL, C, E_>;
+    static_assert(NSTG == 1 || NSTG == 2, "one or two stages");
+    using Cfg = ColTmaCfg<T, LOGL, C, E_, NSTG>;
     using SP = typename Cfg::SP;
     constexpr int E = SP::E, G = SP::G, N = SP::N;
     constexpr int UNITS = sizeof(cpx<T>) / 8;  // 8-byte tensor elements per complex value
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     cpx<T> *const stage0 = reinterpret_cast<cpx<T> *>(smem_raw);
-    uint64_t *const bars = reinterpret_cast<uint64_t *>(smem_raw + 2 * (size_t)Cfg::STAGE * sizeof(cpx<T>));
+    uint64_t *const bars = reinterpret_cast<uint64_t *>(smem_raw + NSTG * (size_t)Cfg::STAGE * sizeof(cpx<T>));
 
     const int s = threadIdx.x % C;
     const int t = threadIdx.x / C;
@@ -160,8 +189,7 @@ __global__ void __launch_bounds__(ColTmaCfg<T, LOGL, C, E_>::THREADS, 1)
     const unsigned lo_mask = (1u << lo_bits) - 1u;
 
     if (threadIdx.x == 0) {
-        mbar_init(&bars[0], 1);
-        mbar_init(&bars[1], 1);
+        for (int i = 0; i < NSTG; i++) mbar_init(&bars[i], 1);
         fence_barrier_init();
     }
     __syncthreads();
@@ -178,8 +206,8 @@ __global__ void __launch_bounds__(ColTmaCfg<T, LOGL, C, E_>::THREADS, 1)
     long long w = blockIdx.x;
     if (threadIdx.x == 0 && w < total) issue(w, 0);
     for (int k = 0; w < total; w += gridDim.x, k++) {
-        const int cur = k & 1;
-        const uint32_t par = (uint32_t)((k >> 1) & 1);
+        const int cur = NSTG == 2 ? (k & 1) : 0;
+        const uint32_t par = (uint32_t)(NSTG == 2 ? ((k >> 1) & 1) : (k & 1));
         const bool ok = mbar_wait(&bars[cur], par);
         if (!__syncthreads_and(ok)) {
             if (threadIdx.x == 0) {
@@ -188,7 +216,7 @@ __global__ void __launch_bounds__(ColTmaCfg<T, LOGL, C, E_>::THREADS, 1)
             }
             return;
         }
-        if (threadIdx.x == 0 && w + gridDim.x < total) {
+        if (NSTG == 2 && threadIdx.x == 0 && w + gridDim.x < total) {
             fence_proxy_async_smem();
             issue(w + gridDim.x, cur ^ 1);
         }
@@ -201,6 +229,15 @@ __global__ void __launch_bounds__(ColTmaCfg<T, LOGL, C, E_>::THREADS, 1)
         cpx<T> *my = S + s * Cfg::PITCH;
         stockham_run<T, LOGL, E_, INV>(
             v, t, [my](int i) -> cpx<T> & { return my[spad<T>(i)]; }, tw, []() { __syncthreads(); });
+        if constexpr (NSTG == 1) {
+            // every thread has read its last exchange values: the buffer
+            // takes the next tile while this one is twiddled and stored
+            __syncthreads();
+            if (threadIdx.x == 0 && w + gridDim.x < total) {
+                fence_proxy_async_smem();
+                issue(w + gridDim.x, 0);
+            }
+        }
         if (col < ncols) {
             cpx<T> *dst = out + b * odist + col + (long long)t * ld_out;
             const long long step = (long long)G * ld_out;
