@@ -57,3 +57,35 @@ def test_two_rank_gloo_shards(world):
         p.join(120)
         assert p.exitcode == 0
     assert q.get(timeout=10) is True
+
+
+def _timing_worker(rank, world, port, q):
+    import sys
+    import torch.distributed as dist
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import bench
+    bench.barrier(world)
+    # each rank's elapsed time differs; the reported time is the slowest
+    got = bench.max_over_ranks(world, 1.0 + rank * 0.25)
+    q.put((rank, got))
+    dist.destroy_process_group()
+
+
+def test_bench_time_is_max_over_ranks():
+    """bench.py reports the slowest rank's time (its barrier and max-reduce
+    run over gloo here, over NCCL under torchrun on GPUs)."""
+    world = 2
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = 30500 + os.getpid() % 1000
+    procs = [ctx.Process(target=_timing_worker, args=(r, world, port, q)) for r in range(world)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(120)
+        assert p.exitcode == 0
+    res = sorted(q.get(timeout=10) for _ in range(world))
+    assert res == [(0, 1.25), (1, 1.25)]
