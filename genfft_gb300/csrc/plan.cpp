@@ -1,5 +1,20 @@
 // plan.cpp -- transform cores (C2C, column, real-input) and their launch
 // sequences.  All device work is stream-ordered on the caller's stream.
+//
+// Path per size (the defaults, each measured on GB300; the environment
+// knobs read below override them):
+//   C2C  n <= 2^14 (fp32) / 2^13 (fp64)  one fused kernel (c2c_fused.cu)
+//        fp32 2^16 .. 2^19               the persistent four-step kernel
+//                                        (fourstep.cuh), one launch a batch
+//        otherwise                       column + row tile launches per
+//                                        workspace group (tiles*.cuh), the
+//                                        widest TMA-pipelined tile that fits
+//   R2C  n/2 within the fused limit      one fused kernel (real.cu)
+//        fp32 half spectrum above it     tile column pass + row pass with
+//                                        the DIT fused (real_4step.cu)
+//        otherwise                       C2C of n/2 + the DIT pass
+//   C2R  n/2 within the fused limit      one fused kernel (c2r.cu)
+//        otherwise                       pre-pass + C2C of n/2, inverse
 #include <algorithm>
 #include <cstdlib>
 #include <string>
