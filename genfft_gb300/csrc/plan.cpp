@@ -40,6 +40,26 @@ static long long env_ll(const char *name, long long dflt)
     return (v && *v) ? std::atoll(v) : dflt;
 }
 
+// the four-step inter-pass twiddle W_N^e = hi[e >> lo_bits] * lo[e & (2^lo_bits - 1)]
+// of N = 2^logn, cached per (type, N)
+static void wn_tables(int dtype, int logn, int *lo_bits, const void **lo, const void **hi)
+{
+    const long long N = 1LL << logn;
+    const int d = dtype;
+    auto fill = [d, N](long long count, long long mul) {
+        return [d, N, count, mul](void *buf) {
+            for (long long e = 0; e < count; e++) {
+                if (d == GFFT_F32) forward_root<float>(e * mul, N, &((float *)buf)[2 * e], &((float *)buf)[2 * e + 1]);
+                else forward_root<double>(e * mul, N, &((double *)buf)[2 * e], &((double *)buf)[2 * e + 1]);
+            }
+        };
+    };
+    *lo_bits = (logn + 1) / 2;
+    const std::string key = "4s/" + std::to_string(dtype) + "/" + std::to_string(logn);
+    *lo = cached_table(key + "/lo", dtype, 1LL << *lo_bits, fill(1LL << *lo_bits, 1));
+    *hi = cached_table(key + "/hi", dtype, N >> *lo_bits, fill(N >> *lo_bits, 1LL << *lo_bits));
+}
+
 static const void *tile_table(int dtype, const TileKernel *k, int logl, int c)
 {
     return cached_table("tile/" + std::to_string(dtype) + "/" + std::to_string(logl) + "/" + std::to_string(c) +
@@ -67,19 +87,8 @@ void C2CCore::init(int dtype_, int logn_, long long batch_hint, int path, bool r
     logB = logn - logA;
     const long long N = 1LL << logn;
     const int d = dtype;
-    auto fill = [d, N](long long count, long long mul) {
-        return [d, N, count, mul](void *buf) {
-            for (long long e = 0; e < count; e++) {
-                if (d == GFFT_F32) forward_root<float>(e * mul, N, &((float *)buf)[2 * e], &((float *)buf)[2 * e + 1]);
-                else forward_root<double>(e * mul, N, &((double *)buf)[2 * e], &((double *)buf)[2 * e + 1]);
-            }
-        };
-    };
     // inter-pass twiddle W_N^e = tw_hi[e >> lo_bits] * tw_lo[e & (2^lo_bits - 1)]
-    lo_bits = (logn + 1) / 2;
-    const std::string key = "4s/" + std::to_string(dtype) + "/" + std::to_string(logn);
-    tw_lo = cached_table(key + "/lo", dtype, 1LL << lo_bits, fill(1LL << lo_bits, 1));
-    tw_hi = cached_table(key + "/hi", dtype, N >> lo_bits, fill(N >> lo_bits, 1LL << lo_bits));
+    wn_tables(dtype, logn, &lo_bits, &tw_lo, &tw_hi);
 
     // the two-launch tile path: always set up (the persistent kernel needs
     // 16-byte aligned inputs for its tensor copies and uses it otherwise)
@@ -299,24 +308,81 @@ void C2CCore::run_stalled(const void *in, void *out, cudaStream_t st) const
 // ---------------------------------------------------------------------------
 // column FFTs
 
-void ColCore::init(int dtype_, int logl_, int variant_)
+void ColCore::init(int dtype_, int logl_, int variant_, bool allow_split)
 {
     dtype = dtype_;
     logl = logl_;
     variant = variant_;
-    if (logl > 12) fail(GFFT_ERR_UNSUPPORTED, "column length above 2^12 is not supported");
+    // plain fp32 columns of 2^13 and 2^14 points run split (no one-launch
+    // tile holds them); 2^10 .. 2^12 on request (GFFT_COL_SPLIT=1): measured
+    // on GB300 for 4096 x 4096 the split column pass is slower (2D C2C 1591
+    // against 1890 GB/s with the one-launch 4096-point tiles)
+    const bool can_split =
+        allow_split && variant == TILE_COL_PLAIN && dtype == GFFT_F32 && logl >= 10 && logl <= 14;
+    if (can_split && (logl > 12 || env_ll("GFFT_COL_SPLIT", 0) != 0)) {
+        l1 = logl / 2;
+        l2 = logl - l1;
+        c1 = l1 <= 6 ? 64 : 32;
+        c2 = l2 <= 6 ? 64 : 32;
+        ka = tile_find(dtype, TILE_COL_TWB, l1, c1);
+        kb = tile_find(dtype, TILE_COL_PLAIN, l2, c2);
+        if (!ka || !kb) fail(GFFT_ERR_UNSUPPORTED, "no split column kernels for this length");
+        tw_a = tile_table(dtype, ka, l1, c1);
+        tw_b = tile_table(dtype, kb, l2, c2);
+        wn_tables(dtype, logl, &lo_bits, &tw_lo, &tw_hi);
+        // bands of columns whose scratch (H x band elements) stays in L2
+        const long long H = 1LL << logl;
+        band = std::max<long long>(64, ((32LL << 20) / (H * (long long)cplx_bytes(dtype))) / 64 * 64);
+        ws_bytes = (size_t)(H * band) * cplx_bytes(dtype);
+        check_cuda(cudaMalloc(&scratch, ws_bytes), "cudaMalloc(column scratch)");
+        split = true;
+        return;
+    }
+    if (logl > 12) fail(GFFT_ERR_UNSUPPORTED, "column length above 2^12 is supported for fp32 plain columns only");
     c = tile_widest(dtype, variant, logl, (int)env_ll("GFFT_COL_MAXC", 16));
     if (!c) fail(GFFT_ERR_UNSUPPORTED, "no column kernel for this length");
     k = tile_find(dtype, variant, logl, c);
     tw = tile_table(dtype, k, logl, c);
 }
 
+void ColCore::release()
+{
+    if (scratch) cudaFree(scratch);
+    scratch = nullptr;
+}
+
 void ColCore::run(int inverse, const void *in, void *out, long long ncols, long long ld_in, long long ld_out,
                   long long batch, long long idist, long long odist, cudaStream_t st, double scale) const
 {
-    check_cuda(launch_colpass(*k, inverse, (ncols + c - 1) / c, batch, in, out, ncols, ld_in, ld_out, idist, odist,
-                              tw, nullptr, nullptr, 0, 0u, st, scale),
-               "launch column FFT");
+    if (!split) {
+        check_cuda(launch_colpass(*k, inverse, (ncols + c - 1) / c, batch, in, out, ncols, ld_in, ld_out, idist,
+                                  odist, tw, nullptr, nullptr, 0, 0u, st, scale),
+                   "launch column FFT");
+        return;
+    }
+    // Column FFT of H = H1 H2 points with rows r = H2 r1 + r2 and bins
+    // k = k1 + H1 k2 (the four-step split along the column):
+    //   A: for each r2 (batch index), H1-point FFTs over r1, times
+    //      W_H^(r2 k1), into scratch[k1][r2][column];
+    //   B: for each k1 (batch index), H2-point FFTs over r2 of the scratch,
+    //      into rows k1 + H1 k2 of the output.
+    // A band of columns at a time, so that the scratch stays in L2; A reads
+    // every row of its band before B writes it, so out may be in.
+    const long long H1 = 1LL << l1, H2 = 1LL << l2;
+    const size_t eb = cplx_bytes(dtype);
+    for (long long b2 = 0; b2 < batch; b2++) {
+        for (long long c0 = 0; c0 < ncols; c0 += band) {
+            const long long wb = std::min(band, ncols - c0);
+            const char *src = static_cast<const char *>(in) + (size_t)(b2 * idist + c0) * eb;
+            char *dst = static_cast<char *>(out) + (size_t)(b2 * odist + c0) * eb;
+            check_cuda(launch_colpass(*ka, inverse, (wb + c1 - 1) / c1, H2, src, scratch, wb, H2 * ld_in, H2 * wb,
+                                      ld_in, wb, tw_a, tw_lo, tw_hi, lo_bits, (unsigned)((H1 * H2) - 1), st, 1.0),
+                       "launch split column pass A");
+            check_cuda(launch_colpass(*kb, inverse, (wb + c2 - 1) / c2, H1, scratch, dst, wb, wb, H1 * ld_out,
+                                      H2 * wb, ld_out, tw_b, nullptr, nullptr, 0, 0u, st, scale),
+                       "launch split column pass B");
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------

@@ -60,7 +60,24 @@ struct ColCore {
     int dtype = 0, logl = 0, variant = 0, c = 0;
     const TileKernel *k = nullptr;
     const void *tw = nullptr;
-    void init(int dtype, int logl, int variant);
+    // split column FFTs (fp32, plain columns of 2^10 .. 2^14 points): each
+    // column of H = H1 * H2 points is two launches of short column FFTs per
+    // band of columns, through an L2-sized scratch (see ColCore::run)
+    bool split = false;
+    int l1 = 0, l2 = 0, c1 = 0, c2 = 0, lo_bits = 0;
+    const TileKernel *ka = nullptr, *kb = nullptr;
+    const void *tw_a = nullptr, *tw_b = nullptr, *tw_lo = nullptr, *tw_hi = nullptr;
+    long long band = 0;  // columns per band
+    void *scratch = nullptr;
+    size_t ws_bytes = 0;
+    // allow_split = false keeps the one-launch tiles (real 2D, whose half-
+    // and full-width results agree bit for bit through the same tiles)
+    void init(int dtype, int logl, int variant, bool allow_split = true);
+    void release();
+    long long launches(long long ncols, long long batch) const
+    {
+        return split ? 2 * batch * ((ncols + band - 1) / band) : 1;
+    }
     void run(int inverse, const void *in, void *out, long long ncols, long long ld_in, long long ld_out,
              long long batch, long long idist, long long odist, cudaStream_t st, double scale = 1.0) const;
 };
@@ -195,5 +212,8 @@ struct gfft_plan_s {
     // whatever their streams: each waits for the last one's event
     std::mutex ws_mu;
     cudaEvent_t ws_last = nullptr;
-    size_t workspace_bytes() const { return c2c.ws_bytes + r2c.c2c.ws_bytes + c2r.c2c.ws_bytes + tc.ws_bytes; }
+    size_t workspace_bytes() const
+    {
+        return c2c.ws_bytes + r2c.c2c.ws_bytes + c2r.c2c.ws_bytes + tc.ws_bytes + col.ws_bytes;
+    }
 };

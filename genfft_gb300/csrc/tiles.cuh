@@ -43,14 +43,16 @@ struct ColCfg {
 // of batch item b = blockIdx.y holds element i at
 //     in [b*idist + row(i)*ld_in + col]       row(i) = BITREV ? bitrev(i) : i
 // and its transform goes to out[b*odist + i*ld_out + col], multiplied by
-// W_N^(col*i) when TW4 (four-step inter-pass twiddle, from the split tables
-// tw_hi[e >> lo_bits] * tw_lo[e & lo_mask], e = col*i mod N).
+// W_N^(f*i) when TWM != 0 (a four-step inter-pass twiddle, from the split
+// tables tw_hi[e >> lo_bits] * tw_lo[e & lo_mask], e = f*i mod N) with
+// f = col (TWM 1: the columns are the second factor) or f = b (TWM 2: the
+// batch index is; one launch covers fewer than 65536 batch items).
 // HERM (real 2D output, RealFFT2D::forward, FFTReal.h:90-103): the tile runs
 // over the W/2+1 non-redundant columns (ncols = W/2+1) and also stores the
 // Hermitian mirror X[(L-i) mod L][W-col] = conj X[i][col] for 0 < col < W/2.
 // Threads are numbered t*C + s, so a warp touches C consecutive columns of
 // a row and global accesses come in C-element runs.
-template <typename T, int LOGL, int C, int E_, bool INV, bool TW4, bool BITREV, bool HERM = false>
+template <typename T, int LOGL, int C, int E_, bool INV, int TWM, bool BITREV, bool HERM = false>
 __global__ void __launch_bounds__(ColCfg<T, LOGL, C, E_>::THREADS)
     k_colpass(const cpx<T> *__restrict__ in, cpx<T> *__restrict__ out, long long ncols, long long ld_in,
               long long ld_out, long long idist, long long odist,
@@ -93,11 +95,11 @@ __global__ void __launch_bounds__(ColCfg<T, LOGL, C, E_>::THREADS)
         if (active) {
             cpx<T> *dst = out + b * odist + col + (long long)t * ld_out;
             const long long step = (long long)G * ld_out;
-            const unsigned ecol = (unsigned)col;
+            const unsigned ecol = TWM == 2 ? (unsigned)b : (unsigned)col;
 #pragma unroll
             for (int q = 0; q < E; q++, dst += step) {
                 cpx<T> val = v[q];
-                if constexpr (TW4) {
+                if constexpr (TWM != 0) {
                     const unsigned e = (ecol * (unsigned)(t + q * G)) & nmask;
                     const cpx<T> w = cmul(ldg_c(tw_hi + (e >> lo_bits)), ldg_c(tw_lo + (e & lo_mask)));
                     val = twmul<INV>(val, w);

@@ -52,15 +52,16 @@ struct TileReg {
         } else {
             using Cfg = ColCfg<T, LOGL, C, E>;
             constexpr bool tw4 = V == TILE_COL_TW4, br = V == TILE_COL_BITREV, herm = V == TILE_COL_HERM;
-            k.fwd = (const void *)&k_colpass<T, LOGL, C, E, false, tw4, br, herm>;
-            k.inv = (const void *)&k_colpass<T, LOGL, C, E, true, tw4, br, herm>;
+            constexpr int twm = tw4 ? 1 : V == TILE_COL_TWB ? 2 : 0;
+            k.fwd = (const void *)&k_colpass<T, LOGL, C, E, false, twm, br, herm>;
+            k.inv = (const void *)&k_colpass<T, LOGL, C, E, true, twm, br, herm>;
             k.threads = Cfg::THREADS;
             k.smem = Cfg::SMEM;
             using TCfg = ColTmaCfg<T, LOGL, C, E>;
             using TCfg1 = ColTmaCfg<T, LOGL, C, E, 1>;
             if constexpr (!br && TCfg::SMEM <= 220 * 1024 && C * sizeof(cpx<T>) % 16 == 0) {
-                k.tma_fwd = (const void *)&k_colpass_tma<T, LOGL, C, E, false, tw4, herm>;
-                k.tma_inv = (const void *)&k_colpass_tma<T, LOGL, C, E, true, tw4, herm>;
+                k.tma_fwd = (const void *)&k_colpass_tma<T, LOGL, C, E, false, twm, herm>;
+                k.tma_inv = (const void *)&k_colpass_tma<T, LOGL, C, E, true, twm, herm>;
                 k.tma_threads = TCfg::THREADS;
                 k.tma_smem = TCfg::SMEM;
                 k.tma_boxr = TCfg::BOXR;
@@ -71,8 +72,8 @@ struct TileReg {
                 // four-step column pass only: measured on GB300, the wider
                 // single-buffered tile beats the narrower double-buffered one
                 // (n = 2^20 .. 2^24: 7-42 %); for 2D columns it does not
-                k.tma_fwd = (const void *)&k_colpass_tma<T, LOGL, C, E, false, tw4, herm, 1>;
-                k.tma_inv = (const void *)&k_colpass_tma<T, LOGL, C, E, true, tw4, herm, 1>;
+                k.tma_fwd = (const void *)&k_colpass_tma<T, LOGL, C, E, false, twm, herm, 1>;
+                k.tma_inv = (const void *)&k_colpass_tma<T, LOGL, C, E, true, twm, herm, 1>;
                 k.tma_threads = TCfg1::THREADS;
                 k.tma_smem = TCfg1::SMEM;
                 k.tma_boxr = TCfg1::BOXR;

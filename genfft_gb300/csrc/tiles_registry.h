@@ -15,7 +15,8 @@ enum TileVariant {
     TILE_COL_PLAIN = 1,   // column FFT, natural-order input
     TILE_COL_BITREV = 2,  // column FFT, bit-reversed row order on input
     TILE_ROW_XPOSE = 3,   // row pass with transposed store
-    TILE_COL_HERM = 4     // column FFT + Hermitian mirror store (real 2D)
+    TILE_COL_HERM = 4,    // column FFT + Hermitian mirror store (real 2D)
+    TILE_COL_TWB = 5      // column pass with the W_N^(batch * row) twiddle (split column FFTs)
 };
 
 struct TileKernel {

@@ -166,7 +166,7 @@ struct ColTmaCfg {
     static constexpr size_t SMEM = NSTG * (size_t)STAGE * sizeof(cpx<T>) + 64;
 };
 
-template <typename T, int LOGL, int C, int E_, bool INV, bool TW4, bool HERM, int NSTG = 2>
+template <typename T, int LOGL, int C, int E_, bool INV, int TWM, bool HERM, int NSTG = 2>
 __global__ void __launch_bounds__(ColTmaCfg<T, LOGL, C, E_, NSTG>::THREADS, 1)
     k_colpass_tma(const __grid_constant__ CUtensorMap map, cpx<T> *__restrict__ out, long long ncols,
                   long long ld_out, long long odist, long long nbatch, const cpx<T> *__restrict__ tw,
@@ -241,11 +241,11 @@ __global__ void __launch_bounds__(ColTmaCfg<T, LOGL, C, E_, NSTG>::THREADS, 1)
         if (col < ncols) {
             cpx<T> *dst = out + b * odist + col + (long long)t * ld_out;
             const long long step = (long long)G * ld_out;
-            const unsigned ecol = (unsigned)col;
+            const unsigned ecol = TWM == 2 ? (unsigned)b : (unsigned)col;
 #pragma unroll
             for (int q = 0; q < E; q++, dst += step) {
                 cpx<T> val = v[q];
-                if constexpr (TW4) {
+                if constexpr (TWM != 0) {
                     const unsigned e = (ecol * (unsigned)(t + q * G)) & nmask;
                     const cpx<T> wv = cmul(ldg_c(tw_hi + (e >> lo_bits)), ldg_c(tw_lo + (e & lo_mask)));
                     val = twmul<INV>(val, wv);

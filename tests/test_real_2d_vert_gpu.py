@@ -373,3 +373,63 @@ def test_real_fft_full_size_2_20_x64(gfft):
         ref = np.fft.rfft(x[b].cpu().numpy().astype(np.float64))
         got = host(y[b])
         assert np.linalg.norm(got - ref) / np.linalg.norm(ref) <= bound(np.float32, n)
+
+
+@pytest.mark.parametrize("h,w,batch", [(1024, 256, 2), (2048, 128, 2), (4096, 64, 1), (8192, 64, 1), (16384, 32, 1)])
+def test_split_column_fft_2d(gfft, oracle, h, w, batch):
+    """2D C2C whose columns (2^10 .. 2^14 points) run as two launches of
+    short column FFTs per band of columns (H = H1 H2, the first with the
+    W_H^(r2 k1) twiddle; the path for 2^13 and 2^14, on request below):
+    both directions against FP64, and against the one-launch column tiles
+    where those exist (H <= 4096); in place."""
+    import os
+    import torch
+    g = torch.Generator(device="cuda").manual_seed(h + w)
+    x = torch.randn(batch, h, w, dtype=torch.complex64, device="cuda", generator=g)
+    x64 = x.cpu().numpy().astype(np.complex128)
+    old = os.environ.get("GFFT_COL_SPLIT")
+    os.environ["GFFT_COL_SPLIT"] = "1"
+    try:
+        for inv in (False, True):
+            got = host(gfft.fft2(x, inverse=inv))
+            ref = np.fft.ifft2(x64) * (h * w) if inv else np.fft.fft2(x64)
+            assert oracle.rel_rms(got, ref) <= bound(np.complex64, h * w), (h, w, inv)
+            if h <= 4096:
+                os.environ["GFFT_COL_SPLIT"] = "0"
+                one = host(gfft.fft2(x, inverse=inv))
+                os.environ["GFFT_COL_SPLIT"] = "1"
+                assert oracle.rel_rms(one, ref) <= bound(np.complex64, h * w)
+                assert oracle.rel_rms(got, one) <= bound(np.complex64, h * w)
+        # in place (the column pass reads each band whole before it writes it)
+        y = x.clone()
+        gfft.fft2(y, out=y)
+        assert np.array_equal(host(y), host(gfft.fft2(x)))
+    finally:
+        if old is None:
+            os.environ.pop("GFFT_COL_SPLIT")
+        else:
+            os.environ["GFFT_COL_SPLIT"] = old
+
+
+@pytest.mark.parametrize("h,cols", [(8192, 3000), (16384, 77)])
+def test_split_column_fft_vert_partial_bands(gfft, oracle, h, cols):
+    """Column FFTs (FFTVert, out of place as in the reference) of 8192 and
+    16384 points (the split path) over column counts that leave partial
+    bands and partial tiles."""
+    import torch
+    g = torch.Generator(device="cuda").manual_seed(cols)
+    x = torch.randn(h, cols, dtype=torch.complex64, device="cuda", generator=g)
+    ref = np.fft.fft(x.cpu().numpy().astype(np.complex128), axis=0)
+    got = host(gfft.fft_vert(x))
+    assert oracle.rel_rms(got, ref) <= bound(np.complex64, h)
+
+
+def test_real_2d_half_odd_stride(gfft, oracle):
+    """Half-width real 2D (W/2+1 = 129 columns, an odd row stride: the plain
+    tile kernels) with 2048-point columns."""
+    import torch
+    g = torch.Generator(device="cuda").manual_seed(3)
+    x = torch.rand(2048, 256, dtype=torch.float32, device="cuda", generator=g)
+    ref = np.fft.rfft2(x.cpu().numpy().astype(np.float64))
+    got = host(gfft.rfft2(x, half=True))
+    assert oracle.rel_rms(got, ref) <= bound(np.float32, 2048 * 256)
