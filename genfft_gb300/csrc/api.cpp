@@ -8,6 +8,7 @@
 // plays that role for the device kernels, with a mutex around creation
 // (the reference's GetInstance is not thread-safe, FFTLevel.h:76-88).
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <cstdlib>
@@ -178,8 +179,17 @@ static void check_layout(const gfft_desc &d)
     }
 }
 
+// a profiler range for the lifetime of a scope (NVTX v3, header-only)
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
+
 static gfft_plan_s *make_plan(const gfft_desc &in)
 {
+    NvtxRange range("gfft plan create");
     gfft_desc d = in;
     validate_desc(d);
     apply_defaults(d);
@@ -353,6 +363,10 @@ static void exec_body(gfft_plan_s &p, int inverse, void *out, const void *in, co
 static void exec_plan(gfft_plan_s &p, int inverse, void *out, const void *in, const Layout &L, cudaStream_t st,
                       double scale = 1.0)
 {
+    // NVTX range per exec (no cost unless a profiler is attached)
+    static const char *const names[] = {"gfft exec C2C", "gfft exec R2C", "gfft exec C2C_2D", "gfft exec R2C_2D",
+                                        "gfft exec VERT"};
+    NvtxRange range(p.d.kind >= 0 && p.d.kind <= 4 ? names[p.d.kind] : "gfft exec");
     if (!p.ws_last) {
         exec_body(p, inverse, out, in, L, st, scale);
         return;
@@ -612,7 +626,10 @@ gfft_status gfft_exec_adjoint(gfft_plan plan, int inverse, void *out, const void
 
 gfft_status gfft_exec_host(gfft_plan plan, int inverse, void *out, const void *in)
 {
-    GFFT_GUARD({ exec_host(*checked(plan), inverse != 0, out, in); });
+    GFFT_GUARD({
+        NvtxRange range("gfft exec host");
+        exec_host(*checked(plan), inverse != 0, out, in);
+    });
 }
 
 gfft_status gfft_plan_launches(gfft_plan plan, int *launches)
@@ -849,6 +866,7 @@ gfft_status gfft_ragged_exec(gfft_ragged plan, int inverse, void *out, const voi
 {
     GFFT_GUARD({
         if (!plan) fail(GFFT_ERR_INVALID_PLAN, "NULL ragged plan");
+        NvtxRange range("gfft ragged exec");
         ragged_exec(*reinterpret_cast<RaggedPlan *>(plan), inverse != 0, out, in, (cudaStream_t)stream, true);
     });
 }
