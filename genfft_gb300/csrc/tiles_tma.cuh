@@ -4,7 +4,9 @@
 // stage buffers: while it transforms the tile in one buffer, the TMA engine
 // fills the other with the next tile, so HBM stays busy through the
 // compute phase (the plain tile kernels load, compute and store in turn and
-// leave HBM idle in between).
+// leave HBM idle in between).  Tiles too wide for two buffers get one
+// (NSTG = 1): the next tile's copy starts as soon as this tile's last
+// shared-memory read is done, and overlaps the rest of its work.
 //   row pass    : the C rows of a tile are C contiguous bulk copies
 //                 (cp.async.bulk, one per row);
 //   column pass : the C x L tile is L/BOXR boxes of a 3D tensor map
