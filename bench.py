@@ -42,6 +42,8 @@ WORKLOADS = {
     "c2c_f64_65536x512": ("c2c", "f64", 1 << 16, 0, 512),
     "c2c_f32_65536x4096": ("c2c", "f32", 1 << 16, 0, 4096),
     "r2c_f32_1048576x64": ("r2c", "f32", 1 << 20, 0, 64),
+    # half-spectrum inverse (no reference counterpart, FFTReal.h:127-130)
+    "c2r_f32_1048576x64": ("c2r", "f32", 1 << 20, 0, 64),
     "c2d_f32_4096x4096": ("c2d", "f32", 4096, 4096, 1),
     "r2d_f32_4096x4096": ("r2d", "f32", 4096, 4096, 1),
     "ragged_f32_10000": ("ragged", "f32", 0, 0, 10000),
@@ -71,6 +73,10 @@ THROTTLE_BITS = {
 }
 
 
+def step_name(kind):
+    return {"c2r": "half-spectrum inverse"}.get(kind, "forward+inverse" if execs_per_step(kind) == 2 else "forward")
+
+
 def metric_name(kind, dtype):
     """The metric both arms report for a workload (GB/s of algorithmic
     bytes: one read of the input and one write of the output per exec)."""
@@ -91,7 +97,7 @@ def algo_bytes_per_transform(kind, dtype, n0, n1):
     cb, rb = elem_bytes(dtype), elem_bytes(dtype) // 2
     if kind == "c2c":
         return 2 * n0 * cb
-    if kind == "r2c":
+    if kind in ("r2c", "c2r"):
         return n0 * rb + (n0 // 2 + 1) * cb
     if kind == "c2d":
         return 2 * n0 * n1 * cb
@@ -104,7 +110,7 @@ def flops_per_transform(kind, n0, n1):
     """5 N log2 N for complex transforms; 2.5 N log2 N for real input."""
     n = n0 * (n1 if kind in ("c2d", "r2d") else 1)
     f = 5.0 * n * math.log2(n) if n > 1 else 0.0
-    return f / 2 if kind in ("r2c", "r2d") else f
+    return f / 2 if kind in ("r2c", "r2d", "c2r") else f
 
 
 def execs_per_step(kind):
@@ -288,6 +294,18 @@ def time_cpu(kind, dtype, n0, n1, batch, budget_s=8.0, max_reps=20):
         sub = max(1, batch // cores)
         run1 = lambda: (fn(p(y), p(x), n0, sub, 0, 1), fn(p(z), p(y), n0, sub, 1, 1))  # noqa: E731
         desc, threads = f"forward+inverse of the full {batch} x {n0} batch", cores
+    elif kind == "c2r":
+        # the reference has no half-spectrum inverse (FFTReal.h:127-130): its
+        # user runs the n-point complex inverse of the Hermitian-extended
+        # spectrum; timed here over the batch, counted as the C2R's bytes
+        x = (rng.standard_normal((batch, n0)) + 1j * rng.standard_normal((batch, n0))).astype(cdt)
+        y = np.empty_like(x)
+        fn = getattr(L, f"{prefix}fft_batch_{s}")
+        run = lambda: fn(p(y), p(x), n0, batch, 1, cores)  # noqa: E731
+        sub = max(1, batch // cores)
+        run1 = lambda: fn(p(y), p(x), n0, sub, 1, 1)  # noqa: E731
+        desc, threads = (f"n-point complex inverse of the full {batch} x {n0} batch (no C2R in the reference)",
+                         cores)
     elif kind == "r2c":
         x = rng.uniform(-1, 1, (batch, n0)).astype(rdt)
         y = np.empty((batch, n0), dtype=cdt)
@@ -315,7 +333,7 @@ def time_cpu(kind, dtype, n0, n1, batch, budget_s=8.0, max_reps=20):
         t0 = time.perf_counter()
         run()
         times.append(time.perf_counter() - t0)
-    nb = batch if kind in ("c2c", "r2c") else 1
+    nb = batch if kind in ("c2c", "r2c", "c2r") else 1
     if kind == "ragged":
         step_bytes = ragged_bytes
     else:
@@ -323,7 +341,7 @@ def time_cpu(kind, dtype, n0, n1, batch, budget_s=8.0, max_reps=20):
     med = statistics.median(times)
     out = {"value": step_bytes / med / 1e9, "unit": "GB/s", "cores": threads, "kind": kindname,
            "sample": f"{len(times)} steps ({desc}), {threads} threads, median step {med * 1e3:.1f} ms"}
-    if kind in ("c2c", "r2c") and threads > 1:
+    if kind in ("c2c", "r2c", "c2r") and threads > 1:
         # the same algorithm on one core, for the per-core figure
         run1()
         t1 = []
@@ -385,7 +403,7 @@ def run_reference(args):
         "ms_per_step": round(med * 1e3, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": dtype, "data": "synthetic",
         "config": {"workload": args.workload, "n": n0, "height": n1 or None, "batch": batch,
-                   "step": "forward+inverse" if execs_per_step(kind) == 2 else "forward",
+                   "step": step_name(kind),
                    "threads": cb["cores"]},
         "cpu_baseline": cb,
         "e2e": {"value": round(cb["value"], 3), "unit": "GB/s", "h2d_bytes_per_step": 0,
@@ -406,6 +424,8 @@ def kernel_name(G, kind, dtype, n0, mode=0, launches=1):
         if fused:
             return "k_c2c_fused"
         return "k_fourstep" if launches == 1 else "k_colpass_tma + k_rowpass_tma"
+    if kind == "c2r":
+        return "k_c2r_fused" if n0 // 2 <= G.max_fused_size(G.F32) else "C2R pre-pass + four-step inverse"
     if kind == "r2c":
         return "k_r2c_fused" if n0 // 2 <= G.max_fused_size(G.F32) else "k_colpass_tma + k_rowpass_dit"
     if kind == "c2d":
@@ -441,6 +461,12 @@ def make_case(G, torch, kind, dtype, n0, n1, batch, rank, mode=0):
         shape_in, shape_out = (batch, n0), (batch, n0 // 2 + 1)
         x = torch.rand(*shape_in, dtype=rdt, device="cuda", generator=gen) * 2 - 1
         plan = G.Plan(G.KIND_R2C, dcode, n0, 0, batch, G.FLAG_HALF_SPECTRUM)
+    elif kind == "c2r":
+        # half spectrum (n/2 + 1 bins, iid N(0,1) re/im) -> n reals, unscaled
+        x = torch.randn(batch, n0 // 2 + 1, dtype=cdt, device="cuda", generator=gen)
+        plan = G.Plan(G.KIND_R2C, dcode, n0, 0, batch, G.FLAG_HALF_SPECTRUM)
+        y = torch.empty(batch, n0, dtype=rdt, device="cuda")
+        return x, y, None, plan, [(y, x, True)]
     else:  # r2d
         shape_in, shape_out = (batch, n1, n0), (batch, n1, n0 // 2 + 1)
         x = torch.rand(*shape_in, dtype=rdt, device="cuda", generator=gen) * 2 - 1
@@ -603,7 +629,8 @@ def run_ours(args):
     kind, dtype, n0, n1, batch, mode = workload(args.workload)
     G.lib()
     x, y, z, plan, execs = make_case(G, torch, kind, dtype, n0, n1, batch, rank, mode)
-    launches_per_exec = plan.launches()
+    # launches of one exec in the direction(s) the step runs
+    launches_per_exec = sum(plan.launches(inv) for _, _, inv in execs) // len(execs)
     stream = torch.cuda.current_stream()
     sp = stream.cuda_stream
 
@@ -653,7 +680,7 @@ def run_ours(args):
     hx = x.cpu().pin_memory()
     hy = torch.empty(y.shape, dtype=y.dtype).pin_memory()
     hz = torch.empty(x.shape, dtype=x.dtype).pin_memory() if z is not None else None
-    hexecs = [(hy, hx, False)] + ([(hz, hy, True)] if z is not None else [])
+    hexecs = [(hy, hx, execs[0][2])] + ([(hz, hy, True)] if z is not None else [])
     for o, i, inv in hexecs:
         plan.exec_host_ptr(o.data_ptr(), i.data_ptr(), inv)
     e2e_steps = max(1, min(K, 5))
@@ -677,6 +704,13 @@ def run_ours(args):
         rel = lambda a: float(np.linalg.norm(a / npts - xr) / np.linalg.norm(xr))  # noqa: E731
         check = rel(z.reshape(batch, -1)[rows].cpu().numpy())
         e2e_check = rel(hz.reshape(batch, -1)[rows].numpy())
+    elif kind == "c2r":
+        # unscaled half-spectrum inverse: n * irfft (DC and Nyquist imaginary
+        # parts ignored, as numpy does)
+        xs = x[rows].cpu().numpy().astype(np.complex128)
+        ref = np.fft.irfft(xs, n=n0) * n0
+        check = float(np.linalg.norm(y[rows].cpu().numpy() - ref) / np.linalg.norm(ref))
+        e2e_check = float(np.linalg.norm(hy[rows].numpy() - ref) / np.linalg.norm(ref))
     else:
         xs = x[rows].cpu().numpy().astype(np.float64)
         ref = np.fft.rfft2(xs) if kind == "r2d" else np.fft.rfft(xs)
@@ -722,7 +756,7 @@ def run_ours(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": dtype,
             "data": "synthetic",
             "config": {"workload": args.workload, "n": n0, "height": n1 or None, "batch": batch,
-                       "step": "forward+inverse" if E == 2 else "forward",
+                       "step": step_name(kind),
                        "layout": "interleaved complex, contiguous batches",
                        "l2": f"{x.numel() * x.element_size() >> 20} MB input per exec > 129 MB L2; no flush"
                              if x.numel() * x.element_size() > (129 << 20) else "input fits L2",

@@ -58,6 +58,7 @@ SIGNATURES = {
     "gfft_exec_adjoint": [_P, _I, _P, _P, _P],
     "gfft_exec_scaled": [_P, _I, ctypes.c_double, _P, _P, _P],
     "gfft_plan_launches": [_P, ctypes.POINTER(_I)],
+    "gfft_plan_launches_dir": [_P, _I, ctypes.POINTER(_I)],
     "gfft_plan_workspace_size": [_P, ctypes.POINTER(ctypes.c_size_t)],
     "gfft_fft_transform": [_I, _I, _LL, _I, _P, _P, _P],
     "gfft_fft_transform_no_scramble": [_I, _I, _LL, _I, _P, _P],
@@ -166,9 +167,10 @@ class Plan:
     def exec_host_ptr(self, out_ptr: int, in_ptr: int, inverse: bool = False):
         _check(lib().gfft_exec_host(self._h, int(inverse), out_ptr, in_ptr))
 
-    def launches(self) -> int:
+    def launches(self, inverse: bool = False) -> int:
+        """Kernel launches one exec makes in that direction."""
         n = _I()
-        _check(lib().gfft_plan_launches(self._h, ctypes.byref(n)))
+        _check(lib().gfft_plan_launches_dir(self._h, int(inverse), ctypes.byref(n)))
         return n.value
 
     def close(self):

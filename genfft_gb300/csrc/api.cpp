@@ -215,6 +215,7 @@ static gfft_plan_s *make_plan(const gfft_desc &in)
             p->r2c.init(d.dtype, ilog2ll(d.n0), half ? 1 : 0, d.batch);
             p->c2r.init(d.dtype, ilog2ll(d.n0), d.batch);
             p->launches = p->r2c.launches(d.batch);
+            p->launches_inv = p->c2r.launches(d.batch);
             break;
         case GFFT_KIND_C2C_2D:
             p->c2c.init(d.dtype, ilog2ll(d.n0), d.batch * d.n1);
@@ -231,6 +232,7 @@ static gfft_plan_s *make_plan(const gfft_desc &in)
             p->launches = (int)p->col.launches(d.n1, d.batch);
             break;
         }
+        if (d.kind != GFFT_KIND_R2C) p->launches_inv = p->launches;
     } catch (...) {
         p->c2c.release();
         p->r2c.release();
@@ -426,12 +428,18 @@ static void exec_adjoint(gfft_plan_s &p, int inverse, void *out, const void *in,
     }
 }
 
-static void io_item_bytes(const gfft_plan_s &p, size_t *ib, size_t *ob)
+// bytes of one transform's input and output in the direction run; the
+// half-spectrum inverse of an R2C plan reads the plan's output layout
+// (bins, odist) and writes its input layout (reals, idist)
+static void io_item_bytes(const gfft_plan_s &p, int inverse, size_t *ib, size_t *ob)
 {
     const gfft_desc &d = p.d;
     const bool real_in = d.kind == GFFT_KIND_R2C || d.kind == GFFT_KIND_R2C_2D;
-    *ib = (size_t)d.idist * (real_in ? real_bytes(d.dtype) : cplx_bytes(d.dtype));
-    *ob = (size_t)d.odist * cplx_bytes(d.dtype);
+    const size_t in_bytes = (size_t)d.idist * (real_in ? real_bytes(d.dtype) : cplx_bytes(d.dtype));
+    const size_t out_bytes = (size_t)d.odist * cplx_bytes(d.dtype);
+    const bool c2r = d.kind == GFFT_KIND_R2C && inverse;
+    *ib = c2r ? out_bytes : in_bytes;
+    *ob = c2r ? in_bytes : out_bytes;
 }
 
 static void exec_host(gfft_plan_s &p, int inverse, void *out, const void *in)
@@ -440,7 +448,7 @@ static void exec_host(gfft_plan_s &p, int inverse, void *out, const void *in)
     if (!in || !out) fail(GFFT_ERR_INVALID_VALUE, "NULL host buffer");
     std::lock_guard<std::mutex> lk(p.host_mu);
     size_t ib, ob;
-    io_item_bytes(p, &ib, &ob);
+    io_item_bytes(p, inverse, &ib, &ob);
     // chunks of about 64 MB (GFFT_HOST_CHUNK_MB), at least one transform
     static const long long chunk = [] {
         const char *v = std::getenv("GFFT_HOST_CHUNK_MB");
@@ -629,6 +637,15 @@ gfft_status gfft_exec_host(gfft_plan plan, int inverse, void *out, const void *i
     GFFT_GUARD({
         NvtxRange range("gfft exec host");
         exec_host(*checked(plan), inverse != 0, out, in);
+    });
+}
+
+gfft_status gfft_plan_launches_dir(gfft_plan plan, int inverse, int *launches)
+{
+    GFFT_GUARD({
+        if (!launches) fail(GFFT_ERR_INVALID_VALUE, "NULL argument");
+        gfft_plan_s *p = checked(plan);
+        *launches = inverse ? p->launches_inv : p->launches;
     });
 }
 

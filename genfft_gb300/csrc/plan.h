@@ -194,7 +194,8 @@ struct gfft_plan_s {
     gfft_desc d;
     unsigned magic = 0x6766u;
     int device = 0;
-    int launches = 0;
+    int launches = 0;      // per forward exec
+    int launches_inv = 0;  // per inverse exec
     gfft::C2CCore c2c;   // C2C; 2D row pass
     gfft::ColCore col;   // 2D column pass; VERT
     gfft::R2CCore r2c;   // R2C; real-2D row pass

@@ -120,8 +120,12 @@ gfft_status gfft_exec_adjoint(gfft_plan plan, int inverse, void *out, const void
  * copies in, transforms and copies out in pipelined chunks, synchronously.
  * Pinned host memory gives full link bandwidth; pageable memory works. */
 gfft_status gfft_exec_host(gfft_plan plan, int inverse, void *out, const void *in);
-/* number of kernel launches one gfft_exec makes (for launch accounting) */
+/* number of kernel launches one forward gfft_exec makes (for launch
+ * accounting) */
 gfft_status gfft_plan_launches(gfft_plan plan, int *launches);
+/* the same for either direction (inverse != 0: the inverse, which for an
+ * R2C plan is the half-spectrum inverse) */
+gfft_status gfft_plan_launches_dir(gfft_plan plan, int inverse, int *launches);
 /* device workspace the plan owns (bytes; 0 for single-kernel sizes) */
 gfft_status gfft_plan_workspace_size(gfft_plan plan, size_t *bytes);
 
