@@ -442,10 +442,48 @@ static void io_item_bytes(const gfft_plan_s &p, int inverse, size_t *ib, size_t 
     *ob = c2r ? in_bytes : out_bytes;
 }
 
+// The host path stages whole transforms: transform b's input is the block
+// of idist elements at b * idist (output likewise), so each transform must
+// lie inside its own block (no batch-interleaved layouts there).
+static void check_host_layout(const gfft_desc &d)
+{
+    const bool half = (d.flags & GFFT_FLAG_HALF_SPECTRUM) != 0;
+    long long in_span = 0, out_span = 0;
+    switch (d.kind) {
+    case GFFT_KIND_C2C:
+        in_span = (d.n0 - 1) * d.istride + 1;
+        out_span = (d.n0 - 1) * d.ostride + 1;
+        break;
+    case GFFT_KIND_R2C:
+        in_span = d.n0;
+        out_span = half ? d.n0 / 2 + 1 : d.n0;
+        break;
+    case GFFT_KIND_C2C_2D:
+        in_span = (d.n1 - 1) * d.istride + d.n0;
+        out_span = (d.n1 - 1) * d.ostride + d.n0;
+        break;
+    case GFFT_KIND_R2C_2D:
+        in_span = (d.n1 - 1) * d.istride + d.n0;
+        out_span = (d.n1 - 1) * d.ostride + (half ? d.n0 / 2 + 1 : d.n0);
+        break;
+    case GFFT_KIND_VERT:
+        in_span = (d.n0 - 1) * d.istride + d.n1;
+        out_span = (d.n0 - 1) * d.ostride + d.n1;
+        break;
+    default:
+        fail(GFFT_ERR_INVALID_PLAN, "plan has no transform kind");
+    }
+    if (in_span > d.idist || out_span > d.odist)
+        fail(GFFT_ERR_UNSUPPORTED,
+             "host buffers: each transform must lie within its own idist / odist block (use device buffers for "
+             "interleaved batches)");
+}
+
 static void exec_host(gfft_plan_s &p, int inverse, void *out, const void *in)
 {
     const gfft_desc &d = p.d;
     if (!in || !out) fail(GFFT_ERR_INVALID_VALUE, "NULL host buffer");
+    check_host_layout(d);
     std::lock_guard<std::mutex> lk(p.host_mu);
     size_t ib, ob;
     io_item_bytes(p, inverse, &ib, &ob);

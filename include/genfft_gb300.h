@@ -118,7 +118,10 @@ gfft_status gfft_exec_scaled(gfft_plan plan, int inverse, double scale, void *ou
 gfft_status gfft_exec_adjoint(gfft_plan plan, int inverse, void *out, const void *in, void *stream);
 /* Same transform on HOST buffers (the reference's calling convention):
  * copies in, transforms and copies out in pipelined chunks, synchronously.
- * Pinned host memory gives full link bandwidth; pageable memory works. */
+ * Pinned host memory gives full link bandwidth; pageable memory works.
+ * Whole transforms are staged, so each must lie inside its own idist /
+ * odist block (GFFT_ERR_UNSUPPORTED for batch-interleaved layouts, which
+ * run on device buffers). */
 gfft_status gfft_exec_host(gfft_plan plan, int inverse, void *out, const void *in);
 /* number of kernel launches one forward gfft_exec makes (for launch
  * accounting) */

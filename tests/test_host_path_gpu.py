@@ -66,3 +66,22 @@ def test_host_2d(gfft):
     p.exec(y, x)
     got = host_exec(p, False, x.cpu().numpy(), (3, 512, 256), np.complex64)
     assert np.array_equal(got.view(np.uint8), y.cpu().numpy().view(np.uint8))
+
+
+def test_host_rejects_interleaved_batches(gfft):
+    """Batch-interleaved layouts (istride = batch, idist = 1) run on device
+    buffers, but the host path, which stages whole transforms, refuses them
+    instead of reading past its staging blocks."""
+    import torch
+    n, batch = 64, 8
+    p = gfft.Plan(gfft.KIND_C2C, gfft.F32, n, 0, batch, 0, batch, 1, batch, 1)
+    x = torch.randn(n, batch, dtype=torch.complex64, device="cuda")  # element q of transform b at q * batch + b
+    y = torch.empty_like(x)
+    p.exec(y, x)
+    ref = np.fft.fft(x.cpu().numpy().astype(np.complex128), axis=0)
+    assert np.linalg.norm(y.cpu().numpy() - ref) / np.linalg.norm(ref) <= 2e-7 * 6
+    hx = x.cpu().numpy()
+    hy = np.empty_like(hx)
+    with pytest.raises(gfft.GFFTError) as e:
+        p.exec_host_ptr(hy.ctypes.data, hx.ctypes.data)
+    assert e.value.name == "GFFT_ERR_UNSUPPORTED"
