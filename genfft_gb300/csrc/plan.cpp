@@ -315,8 +315,8 @@ void ColCore::init(int dtype_, int logl_, int variant_, bool allow_split)
     variant = variant_;
     // plain fp32 columns of 2^13 and 2^14 points run split (no one-launch
     // tile holds them); 2^10 .. 2^12 on request (GFFT_COL_SPLIT=1): measured
-    // on GB300 for 4096 x 4096 the split column pass is slower (2D C2C 1591
-    // against 1890 GB/s with the one-launch 4096-point tiles)
+    // on GB300 for 4096 x 4096 the split column pass is no faster (2D C2C
+    // 1887 against 1899 GB/s with the one-launch 4096-point tiles)
     const bool can_split =
         allow_split && variant == TILE_COL_PLAIN && dtype == GFFT_F32 && logl >= 10 && logl <= 14;
     if (can_split && (logl > 12 || env_ll("GFFT_COL_SPLIT", 0) != 0)) {
@@ -330,9 +330,14 @@ void ColCore::init(int dtype_, int logl_, int variant_, bool allow_split)
         tw_a = tile_table(dtype, ka, l1, c1);
         tw_b = tile_table(dtype, kb, l2, c2);
         wn_tables(dtype, logl, &lo_bits, &tw_lo, &tw_hi);
-        // bands of columns whose scratch (H x band elements) stays in L2
+        // bands of columns, H x band elements of scratch each
+        // (GFFT_COL_BAND_MB): measured on GB300 at 4096 x 4096 the launch
+        // count dominates, not the scratch's L2 residency (2D C2C 1238 /
+        // 1592 / 1747 / 1887 GB/s with 16 / 32 / 64 / 128 MB bands), so the
+        // default is 128 MB
         const long long H = 1LL << logl;
-        band = std::max<long long>(64, ((32LL << 20) / (H * (long long)cplx_bytes(dtype))) / 64 * 64);
+        const long long band_bytes = std::max<long long>(1, env_ll("GFFT_COL_BAND_MB", 128)) << 20;
+        band = std::max<long long>(64, (band_bytes / (H * (long long)cplx_bytes(dtype))) / 64 * 64);
         ws_bytes = (size_t)(H * band) * cplx_bytes(dtype);
         check_cuda(cudaMalloc(&scratch, ws_bytes), "cudaMalloc(column scratch)");
         split = true;
@@ -366,7 +371,7 @@ void ColCore::run(int inverse, const void *in, void *out, long long ncols, long 
     //      W_H^(r2 k1), into scratch[k1][r2][column];
     //   B: for each k1 (batch index), H2-point FFTs over r2 of the scratch,
     //      into rows k1 + H1 k2 of the output.
-    // A band of columns at a time, so that the scratch stays in L2; A reads
+    // A band of columns at a time (the scratch holds one band); A reads
     // every row of its band before B writes it, so out may be in.
     const long long H1 = 1LL << l1, H2 = 1LL << l2;
     const size_t eb = cplx_bytes(dtype);

@@ -62,7 +62,7 @@ struct ColCore {
     const void *tw = nullptr;
     // split column FFTs (fp32, plain columns of 2^10 .. 2^14 points): each
     // column of H = H1 * H2 points is two launches of short column FFTs per
-    // band of columns, through an L2-sized scratch (see ColCore::run)
+    // band of columns, through a scratch of one band (see ColCore::run)
     bool split = false;
     int l1 = 0, l2 = 0, c1 = 0, c2 = 0, lo_bits = 0;
     const TileKernel *ka = nullptr, *kb = nullptr;
