@@ -170,8 +170,10 @@ void C2CCore::init(int dtype_, int logn_, long long batch_hint, int path, bool r
         algo = 3;
         return;
     }
-    // transforms per launch pair, bounded by the workspace budget
-    const long long budget = env_ll("GFFT_WS_BUDGET_MB", 512) << 20;
+    // transforms per launch pair, bounded by the workspace budget: fewer,
+    // larger launch pairs (measured on GB300, 1 GB against 512 MB: +2 % for
+    // n = 2^20 .. 2^23, e.g. 2^22 x 32 in one pair instead of two)
+    const long long budget = env_ll("GFFT_WS_BUDGET_MB", 1024) << 20;
     group = std::max<long long>(1, budget / (N * (long long)cplx_bytes(dtype)));
     group = std::min(group, std::max<long long>(1, batch_hint));
     ws_bytes = (size_t)(group * N) * cplx_bytes(dtype);
