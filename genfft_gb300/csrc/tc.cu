@@ -42,6 +42,7 @@
 #include <cuda_fp16.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <set>
@@ -544,7 +545,12 @@ void TCCore::init(int mode_, int logn_, long long batch_hint)
         tw2 = cached_table("tc/w4096lo", GFFT_F32, 32, [](void *buf) { tcf::fill_pairs(4096, 16, (float *)buf); });
     if (logn == 16) {
         tw2 = cached_table("tc/w65536lo", GFFT_F32, 512, [](void *buf) { tcf::fill_pairs(65536, 256, (float *)buf); });
-        group = std::max<long long>(1, std::min<long long>(std::max<long long>(1, batch_hint), 1024));
+        // transforms per column/row launch pair, within the workspace budget
+        // of the tile launches (GFFT_WS_BUDGET_MB, 1 GB: 2048 transforms)
+        const char *v = std::getenv("GFFT_WS_BUDGET_MB");
+        const long long budget_mb = (v && *v) ? std::max(1LL, std::atoll(v)) : 1024;
+        const long long cap = std::max<long long>(1, (budget_mb << 20) / (65536 * 8));
+        group = std::max<long long>(1, std::min<long long>(std::max<long long>(1, batch_hint), cap));
         ws_bytes = (size_t)group * 65536 * 8;
         check_cuda(cudaMalloc(&ws, ws_bytes), "cudaMalloc(workspace)");
     }
