@@ -582,7 +582,10 @@ static gfft_plan_s *cached_plan(int kind, int dtype, long long n0, long long n1,
     d.flags = flags;
     d.n0 = n0;
     d.n1 = n1;
-    d.batch = 1 << 20;  // sizes the workspace for full groups; the batch is per call
+    // the batch is per call; this one only sizes the workspace: full groups
+    // within 512 MB (these plans live until exit, one per size used)
+    const long long elems = std::max<long long>(1, n0) * std::max<long long>(1, n1);
+    d.batch = std::max<long long>(1, (512LL << 20) / (elems * (long long)cplx_bytes(dtype)));
     gfft_plan_s *p = make_plan(d);
     if (p->workspace_bytes() > 0) {
         cudaError_t e = cudaEventCreateWithFlags(&p->ws_last, cudaEventDisableTiming);
