@@ -615,6 +615,103 @@ def run_ragged(args):
     return 0
 
 
+def tc_accuracy(G, torch, x, y, plan, n0, batch, avg_exec_ms, stream, mode):
+    """Tensor-core workload: its error and the plain fp32 path's error
+    against an FP64 FFT of the first and last rows, and the plain path's
+    time on the same full batch."""
+    import numpy as np
+    rows = [0, batch - 1]
+    xs = x[rows].cpu().numpy().astype(np.complex128)
+    exact = np.fft.fft(xs)
+    err = lambda a: float(np.linalg.norm(a - exact) / np.linalg.norm(exact))  # noqa: E731
+    pp = G.Plan(G.KIND_C2C, G.F32, n0, 0, len(rows))
+    xp = x[rows].contiguous()
+    yp = torch.empty_like(xp)
+    pp.exec(yp, xp)
+    plain = G.Plan(G.KIND_C2C, G.F32, n0, 0, batch)
+    for _ in range(2):
+        plain.exec(y, x)
+    a_ev, b_ev = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a_ev.record(stream)
+    for _ in range(5):
+        plain.exec(y, x)
+    b_ev.record(stream)
+    torch.cuda.synchronize()
+    plain_ms = a_ev.elapsed_time(b_ev) / 5
+    plan.exec(y, x)
+    torch.cuda.synchronize()
+    out = {"rel_rms_vs_fp64": err(y[rows].cpu().numpy()),
+           "plain_rel_rms_vs_fp64": err(yp.cpu().numpy()),
+           "bound": 2e-7 * math.log2(n0), "rows": rows,
+           "mode": MODE_NAMES[mode], "exec_ms": round(avg_exec_ms, 5),
+           "plain_exec_ms": round(plain_ms, 5),
+           "tc_over_plain_time": round(avg_exec_ms / plain_ms, 3)}
+    del plain, pp
+    return out
+
+
+# measured beside the headline in the default run (one GPU): the other fp32
+# C2C size the metric names and the tensor-core comparison at equal error
+COMPANIONS = ["c2c_f32_4194304x32", "tcfp16_f32_65536x4096", "tcbf16_f32_65536x4096"]
+
+
+def companion(G, torch, name, steps, warmup, dev):
+    """One short device-resident measurement of another workload: at most
+    `steps` timed forward+inverse steps with an event pair around every
+    exec; the buffers are freed before it returns."""
+    import numpy as np
+    kind, dtype, n0, n1, batch, mode = workload(name)
+    x, y, z, plan, execs = make_case(G, torch, kind, dtype, n0, n1, batch, 0, mode)
+    launches_per_exec = sum(plan.launches(inv) for _, _, inv in execs) // len(execs)
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    for _ in range(max(3, warmup)):
+        for o, i, inv in execs:
+            plan.exec_ptr(o.data_ptr(), i.data_ptr(), inv, sp)
+    torch.cuda.synchronize()
+    E = len(execs)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(E * steps)]
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev) as clk:
+        start.record(stream)
+        for k in range(steps):
+            for e, (o, inp, inv) in enumerate(execs):
+                ev[E * k + e][0].record(stream)
+                plan.exec_ptr(o.data_ptr(), inp.data_ptr(), inv, sp)
+                ev[E * k + e][1].record(stream)
+        stop.record(stream)
+        torch.cuda.synchronize()
+    ms = start.elapsed_time(stop)
+    avg_exec_ms = statistics.mean(a.elapsed_time(b) for a, b in ev)
+    per_transform = algo_bytes_per_transform(kind, dtype, n0, n1)
+    peak, peak_src = measured_peak()
+    achieved = batch * per_transform / (avg_exec_ms / 1e3) / 1e9
+    out = {"metric": metric_name(kind, dtype) + (f", {MODE_NAMES[mode]} tensor-core path" if mode else ""),
+           "value": round(steps * E * batch * per_transform / (ms / 1e3) / 1e9, 2), "unit": "GB/s",
+           "steps": steps, "warmup": max(3, warmup), "ms_per_step": round(ms / steps, 4),
+           "config": {"n": n0, "batch": batch, "step": step_name(kind),
+                      "l2": f"{x.numel() * x.element_size() >> 20} MB input per exec > 129 MB L2; no flush"},
+           "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                        "frac": round(achieved / peak, 4), "traffic": traffic_from_profile(name),
+                        "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)" if peak_src == "measured"
+                        else "fallback 6800 GB/s",
+                        "kernel": kernel_name(G, kind, dtype, n0, mode, launches_per_exec),
+                        "launches_per_exec": launches_per_exec, "avg_exec_ms": round(avg_exec_ms, 5),
+                        "algorithmic_bytes_per_exec": batch * per_transform},
+           "gpu_launches": E * steps * launches_per_exec, "clocks": clk.summary()}
+    rows = [0, batch - 1]
+    xr = x[rows].cpu().numpy()
+    if z is not None:
+        zr = z[rows].cpu().numpy()
+        out["check"] = float(np.linalg.norm(zr / n0 - xr) / np.linalg.norm(xr))
+    if mode:
+        out["accuracy"] = tc_accuracy(G, torch, x, y, plan, n0, batch, avg_exec_ms, stream, mode)
+    del x, y, z, plan, execs
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    return out
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -717,36 +814,7 @@ def run_ours(args):
         check = float(np.linalg.norm(y[rows].cpu().numpy() - ref) / np.linalg.norm(ref))
         e2e_check = float(np.linalg.norm(hy[rows].numpy() - ref) / np.linalg.norm(ref))
 
-    accuracy = None
-    if mode:
-        rows = [0, batch - 1]
-        xs = x[rows].cpu().numpy().astype(np.complex128)
-        exact = np.fft.fft(xs)
-        err = lambda a: float(np.linalg.norm(a - exact) / np.linalg.norm(exact))  # noqa: E731
-        pp = G.Plan(G.KIND_C2C, G.F32, n0, 0, len(rows))
-        xp = x[rows].contiguous()
-        yp = torch.empty_like(xp)
-        pp.exec(yp, xp)
-        # plain path time on the same full batch, for the tensor-core comparison
-        plain = G.Plan(G.KIND_C2C, G.F32, n0, 0, batch)
-        for _ in range(2):
-            plain.exec(y, x)
-        a_ev, b_ev = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a_ev.record(stream)
-        for _ in range(5):
-            plain.exec(y, x)
-        b_ev.record(stream)
-        torch.cuda.synchronize()
-        plain_ms = a_ev.elapsed_time(b_ev) / 5
-        plan.exec(y, x)
-        torch.cuda.synchronize()
-        accuracy = {"rel_rms_vs_fp64": err(y[rows].cpu().numpy()),
-                    "plain_rel_rms_vs_fp64": err(yp.cpu().numpy()),
-                    "bound": 2e-7 * math.log2(n0), "rows": rows,
-                    "mode": MODE_NAMES[mode], "exec_ms": round(avg_exec_ms, 5),
-                    "plain_exec_ms": round(plain_ms, 5),
-                    "tc_over_plain_time": round(avg_exec_ms / plain_ms, 3)}
-        del plain, pp
+    accuracy = tc_accuracy(G, torch, x, y, plan, n0, batch, avg_exec_ms, stream, mode) if mode else None
     if rank == 0:
         line = {
             "metric": metric_name(kind, dtype)
@@ -781,10 +849,36 @@ def run_ours(args):
         if not args.no_cpu and world == 1:
             cb, _, _ = time_cpu(kind, dtype, n0, n1, batch, budget_s=args.cpu_budget, max_reps=5)
             line["cpu_baseline"] = cb
+        if args.workload == DEFAULT and world == 1 and not args.no_companions:
+            del x, y, z, hx, hy, hz, hexecs, execs
+            torch.cuda.synchronize()
+            torch.cuda.empty_cache()
+            line["companions"] = {}
+            for name in COMPANIONS:
+                line["companions"][name] = companion(G, torch, name, min(10, max(1, K)), args.warmup, dev)
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+    return 0
+
+
+def run_peaks():
+    """FMA throughput of the device (gfft_diag_fma_rate): the FP64 rate is
+    the fp64 kernels' compute roof; fp32 against packed fp32x2 shows whether
+    the packed form raises the FP32 rate or only saves issue slots."""
+    import torch
+
+    import genfft_gb300 as G
+    torch.cuda.set_device(0)
+    L = G.lib()
+    out = {"probe": "independent FMA chains, 8 per thread, CUDA events, best of 5"}
+    for which, name in ((0, "fp32_fma"), (1, "fp32x2_fma"), (2, "fp64_fma")):
+        tf, ms = ctypes.c_double(), ctypes.c_double()
+        with ClockSampler(0) as clk:
+            G._check(L.gfft_diag_fma_rate(which, ctypes.byref(tf), ctypes.byref(ms)))
+        out[name] = {"tflops": round(tf.value, 3), "ms": round(ms.value, 4), "clocks": clk.summary()}
+    print(json.dumps(out), flush=True)
     return 0
 
 
@@ -797,9 +891,15 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT)
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--cpu-budget", type=float, default=8.0)
+    ap.add_argument("--no-companions", action="store_true",
+                    help="default workload: skip the 2^22 and tensor-core companion measurements")
     ap.add_argument("--batch", type=int, default=0,
                     help="override the workload's batch (ragged: transform count); for small profiling captures")
+    ap.add_argument("--peaks", action="store_true",
+                    help="print the device's fp32 / packed fp32x2 / fp64 FMA rates (one JSON line) and exit")
     args = ap.parse_args()
+    if args.peaks:
+        return run_peaks()
     global BATCH_OVERRIDE
     BATCH_OVERRIDE = args.batch or None
     if args.impl == "reference":

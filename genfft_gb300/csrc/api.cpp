@@ -42,7 +42,7 @@ void check_cuda(cudaError_t e, const char *what)
     }
 }
 
-static void check_device()
+void check_device()
 {
     int dev = 0;
     check_cuda(cudaGetDevice(&dev), "cudaGetDevice");

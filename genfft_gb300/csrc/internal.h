@@ -20,6 +20,8 @@ struct Error {
 [[noreturn]] void fail(gfft_status st, const std::string &msg);
 void set_last_error(const char *msg);  // the thread's gfft_last_error() text
 void check_cuda(cudaError_t e, const char *what);
+// GFFT_ERR_ARCH unless the current device is an sm_103 (GB300)
+void check_device();
 
 // ---- fused single-kernel C2C (c2c_fused.cu) ------------------------------
 struct FusedC2CArgs {

@@ -28,6 +28,7 @@
 #include <cstdint>
 #include <cstring>
 #include <mutex>
+#include <new>
 #include <vector>
 
 #include "internal.h"
@@ -116,8 +117,13 @@ void setup_device(int dev, Setup &s)
         s.kcol[n] = tile_find(GFFT_F32, TILE_COL_TW4, la, s.ccol[n]);
         s.krow[n] = tile_find(GFFT_F32, TILE_ROW_XPOSE, lb, s.crow[n]);
         if (!s.kcol[n] || !s.krow[n]) fail(GFFT_ERR_UNSUPPORTED, "no tile kernel");
-        // tile kernels of the same length must share one Stockham table
+        // tile kernels of the same length must share one Stockham table:
+        // the column kernel's own table must equal the one stored for la
         if ((long long)s.kcol[n]->twcount != stockham_tw(la)) fail(GFFT_ERR_UNSUPPORTED, "tile table mismatch");
+        std::vector<cpx<float>> mine((size_t)stockham_tw(la));
+        s.kcol[n]->fill(mine.data());
+        if (std::memcmp(mine.data(), host.data() + s.stock_off[la], mine.size() * sizeof(cpx<float>)) != 0)
+            fail(GFFT_ERR_UNSUPPORTED, "tile table mismatch");
         for (const TileKernel *k : {s.kcol[n], s.krow[n]})
             for (const void *fn : {k->fwd, k->inv})
                 if (k->smem > 48 * 1024)
@@ -147,6 +153,7 @@ extern "C" gfft_status gfft_fft_transform_noalloc(int dtype, int n, long long ba
         if (batch < 1) fail(GFFT_ERR_INVALID_SIZE, "batch must be >= 1");
         if (!in || !out) fail(GFFT_ERR_INVALID_VALUE, "NULL pointer");
         if (((uintptr_t)in | (uintptr_t)out) % 8) fail(GFFT_ERR_ALIGN, "pointers must be 8-byte aligned");
+        check_device();
         int dev = 0;
         check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
         if (dev < 0 || dev >= NA_MAX_DEVICES) fail(GFFT_ERR_UNSUPPORTED, "device ordinal out of range");
@@ -191,6 +198,9 @@ extern "C" gfft_status gfft_fft_transform_noalloc(int dtype, int n, long long ba
     } catch (const Error &e) {
         set_last_error(e.msg.c_str());
         return e.status;
+    } catch (const std::bad_alloc &) {
+        set_last_error("host allocation failed");
+        return GFFT_ERR_ALLOC;
     } catch (...) {
         set_last_error("unexpected exception");
         return GFFT_ERR_INVALID_VALUE;

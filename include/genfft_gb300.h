@@ -240,6 +240,14 @@ gfft_status gfft_ragged_elements(gfft_ragged plan, long long *elements);
  * for tensor-core MMAs gave up) and GFFT_ERR_TIMEOUT.  Reading resets it. */
 gfft_status gfft_device_error(int *code);
 
+/* Arithmetic-rate probe of the current device (no counterpart in the
+ * reference): times independent fused multiply-add chains with CUDA events
+ * on a private stream.  which = 0 fp32 fma, 1 packed fp32x2 fma
+ * (fma.rn.f32x2), 2 fp64 fma; *tflops counts two flops per FMA lane, *ms is
+ * the best of five timed launches.  Allocates a 4-byte device buffer; it is
+ * the denominator of the fp64 kernels' roofline. */
+gfft_status gfft_diag_fma_rate(int which, double *tflops, double *ms);
+
 const char *gfft_status_string(gfft_status status);
 /* message of the last failed call on this thread ("" if none) */
 const char *gfft_last_error(void);

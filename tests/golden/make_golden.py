@@ -1,6 +1,6 @@
 """Generate the golden vectors in tests/golden/genfft_ref_golden.npz.
 
-Run here (x86 host with the reference tree present):
+Run on an x86 host with a genFFT checkout, named by GENFFT_REFERENCE_DIR:
     make -C oracle ref && python tests/golden/make_golden.py
 
 Every expected output comes from the UNMODIFIED reference genFFT, compiled

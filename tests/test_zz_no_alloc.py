@@ -41,6 +41,31 @@ def test_noalloc_matches_allocating_entry_point(gfft, logn, batch):
             assert torch.isfinite(out.view(torch.float32)).all()
 
 
+@pytest.mark.parametrize("logn,batch", [(16, 4), (22, 3)])
+def test_noalloc_in_place_and_guard_bands(gfft, logn, batch):
+    # out == in (each group's column pass reads its transforms before the
+    # row pass writes them), and nothing written outside the output: the
+    # output sits between NaN guard bands that must survive
+    import torch
+    L = gfft.lib()
+    n, pad = 1 << logn, 4096
+    g = torch.Generator(device="cuda").manual_seed(100 + logn)
+    x = torch.randn(batch, n, dtype=torch.complex64, device="cuda", generator=g)
+    st = torch.cuda.current_stream().cuda_stream
+    for inverse in (0, 1):
+        ref = torch.empty_like(x)
+        gfft._check(L.gfft_fft_transform(0, n, batch, inverse, ref.data_ptr(), x.data_ptr(), st))
+        buf = torch.full((batch * n + 2 * pad,), float("nan"), dtype=torch.complex64, device="cuda")
+        body = buf[pad:pad + batch * n]
+        body.copy_(x.reshape(-1))
+        gfft._check(L.gfft_fft_transform_noalloc(0, n, batch, inverse, body.data_ptr(), body.data_ptr(), st))
+        torch.cuda.synchronize()
+        assert torch.isnan(buf[:pad].view(torch.float32)).all()
+        assert torch.isnan(buf[pad + batch * n:].view(torch.float32)).all()
+        err = rel_rms(body.reshape(batch, n), ref)
+        assert err <= 2e-7 * logn, (logn, inverse, err)
+
+
 def test_noalloc_rejects_what_it_cannot_hold(gfft):
     import torch
     L = gfft.lib()
