@@ -33,7 +33,8 @@ def test_noalloc_matches_allocating_entry_point(gfft, logn, batch):
         ref = torch.empty_like(x)
         gfft._check(L.gfft_fft_transform(0, n, batch, inverse, ref.data_ptr(), x.data_ptr(), st))
         for call in range(2):  # two calls in a row share the scratch
-            out = torch.full_like(x, float("nan"))
+            out = torch.full((2 * batch * n,), float("nan"), dtype=torch.float32,
+                             device="cuda").view(torch.complex64).reshape(batch, n)
             gfft._check(L.gfft_fft_transform_noalloc(0, n, batch, inverse, out.data_ptr(), x.data_ptr(), st))
             torch.cuda.synchronize()
             err = rel_rms(out, ref)
@@ -55,7 +56,10 @@ def test_noalloc_in_place_and_guard_bands(gfft, logn, batch):
     for inverse in (0, 1):
         ref = torch.empty_like(x)
         gfft._check(L.gfft_fft_transform(0, n, batch, inverse, ref.data_ptr(), x.data_ptr(), st))
-        buf = torch.full((batch * n + 2 * pad,), float("nan"), dtype=torch.complex64, device="cuda")
+        # NaN in both lanes of every guard element (a complex fill of nan
+        # would leave the imaginary parts at zero)
+        buf = torch.full((2 * (batch * n + 2 * pad),), float("nan"), dtype=torch.float32,
+                         device="cuda").view(torch.complex64)
         body = buf[pad:pad + batch * n]
         body.copy_(x.reshape(-1))
         gfft._check(L.gfft_fft_transform_noalloc(0, n, batch, inverse, body.data_ptr(), body.data_ptr(), st))
