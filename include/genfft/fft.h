@@ -17,9 +17,17 @@
 // Semantics follow the reference: calls are synchronous and the inverse is
 // unscaled.  Buffers may be host memory (as with the reference: they are
 // staged through device memory owned by the object) or device memory (the
-// transform runs in place on the GPU, no copies).  The factory template
-// parameter of the reference classes is not needed: the backend is fixed.
-// Errors throw genfft::gb300_error (the reference asserts instead).
+// transform runs in place on the GPU, no copies).  Errors throw
+// genfft::gb300_error (the reference asserts instead).
+//
+// The classes keep the reference's factory template parameters (fft.h:56,
+// 117, 173, FFTReal.h:188), defaulting to genfft::backend::{GetImpl,
+// GetVertImpl, GetDITImpl}, which here name the GB300 backend
+// (gb300_backend.h).  With those factories the classes call the C ABI
+// directly (no host bit reversal: the kernels are Stockham auto-sort).  With
+// any other factory they run the reference's own algorithm on host
+// buffers: bit-reversal copy (FFTUtil.h:51-98), then the factory's backend
+// object, as fft.h:80-171 and FFTReal.h:204-213 do.
 #ifndef GENFFT_GB300_FFT_H
 #define GENFFT_GB300_FFT_H
 
@@ -27,110 +35,65 @@
 
 #include <complex>
 #include <cstddef>
-#include <stdexcept>
+#include <memory>
 #include <string>
 
-#include "../genfft_gb300.h"
+#include "gb300_backend.h"
 
 namespace genfft {
 
-using stride_t = ptrdiff_t;
-using index_t = int;
-
-struct gb300_error : std::runtime_error {
-    gfft_status status;
-    gb300_error(gfft_status s, const std::string &what) : std::runtime_error(what), status(s) {}
-};
+/// the backend alias set of the reference (FFTBackend.h:40-70), here the GPU
+namespace backend {
+using gb300::GetDITImpl;
+using gb300::GetImpl;
+using gb300::GetVertImpl;
+}  // namespace backend
 
 namespace gb300 {
-
-template <class T>
-constexpr int dtype()
+namespace detail {
+inline int rev_bits(int i, int bits)
 {
-    static_assert(sizeof(T) == 4 || sizeof(T) == 8, "genfft::gb300 supports float and double");
-    return sizeof(T) == 4 ? GFFT_F32 : GFFT_F64;
+    int r = 0;
+    for (int b = 0; b < bits; b++) r |= ((i >> b) & 1) << (bits - 1 - b);
+    return r;
 }
-
-inline void check(gfft_status s)
+inline int log2i(int n)
 {
-    if (s != GFFT_OK) throw gb300_error(s, std::string(gfft_status_string(s)) + ": " + gfft_last_error());
+    int l = 0;
+    while ((1 << l) < n) l++;
+    return l;
 }
-
-inline void check_cuda(cudaError_t e)
+// out[rev(i)] = f(i) for i < n: the reference's scramble (FFTUtil.h:51-83)
+template <class F>
+void scramble_by(int n, F &&f)
 {
-    if (e != cudaSuccess) throw gb300_error(GFFT_ERR_CUDA, cudaGetErrorString(e));
+    const int bits = log2i(n);
+    for (int i = 0; i < n; i++) f(rev_bits(i, bits), i);
 }
-
-inline bool on_device(const void *p)
-{
-    cudaPointerAttributes a;
-    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
-        cudaGetLastError();
-        return false;
-    }
-    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
-}
-
-// Device staging buffer owned by a transform object (grown on demand).
-class Buffer {
-public:
-    Buffer() = default;
-    Buffer(const Buffer &) = delete;
-    Buffer &operator=(const Buffer &) = delete;
-    Buffer(Buffer &&o) noexcept : p_(o.p_), n_(o.n_) { o.p_ = nullptr, o.n_ = 0; }
-    ~Buffer() { if (p_) cudaFree(p_); }
-    void *get(size_t bytes)
-    {
-        if (bytes > n_) {
-            if (p_) cudaFree(p_);
-            p_ = nullptr;
-            n_ = 0;
-            check_cuda(cudaMalloc(&p_, bytes));
-            n_ = bytes;
-        }
-        return p_;
-    }
-
-private:
-    void *p_ = nullptr;
-    size_t n_ = 0;
-};
-
-// Runs `op(dev_out, dev_in)` on device pointers, staging host buffers:
-// in_bytes are copied in, out_bytes copied back, then synchronised.
-template <class Op>
-void staged(void *out, size_t out_bytes, const void *in, size_t in_bytes, Buffer &bo, Buffer &bi, Op op,
-            bool out_preload = false)
-{
-    const bool din = on_device(in), dout = on_device(out);
-    const void *dev_in = in;
-    void *dev_out = out;
-    if (!din) {
-        void *b = bi.get(in_bytes);
-        check_cuda(cudaMemcpy(b, in, in_bytes, cudaMemcpyHostToDevice));
-        dev_in = b;
-    }
-    if (!dout) {
-        dev_out = (in == out && !din) ? const_cast<void *>(dev_in) : bo.get(out_bytes);
-        if (out_preload && dev_out != dev_in) check_cuda(cudaMemcpy(dev_out, out, out_bytes, cudaMemcpyHostToDevice));
-    }
-    op(dev_out, dev_in);
-    check_cuda(cudaDeviceSynchronize());
-    if (!dout) check_cuda(cudaMemcpy(out, dev_out, out_bytes, cudaMemcpyDeviceToHost));
-}
-
+}  // namespace detail
 }  // namespace gb300
 
 /// 1D FFT of densely packed data (reference fft.h:56-113)
-template <class T>
+template <class T, FFTImplFactory<T> *factory = backend::GetImpl>
 struct FFT {
+    /// true when the factory is the GB300 backend: the direct C-ABI path
+    static constexpr bool native = factory == static_cast<FFTImplFactory<T> *>(&gb300::GetImpl<T>);
+
     FFT() = default;
-    explicit FFT(int n) : n(n) { gb300::check(n > 0 && (n & (n - 1)) == 0 ? GFFT_OK : GFFT_ERR_INVALID_SIZE); }
+    explicit FFT(int n) : n(n)
+    {
+        gb300::check(n > 0 && (n & (n - 1)) == 0 ? GFFT_OK : GFFT_ERR_INVALID_SIZE);
+        if (!native) impl = factory(n, T());
+    }
 
     /// in place, bit-reversed input, natural-order output (fft.h:69-73)
     template <bool inv>
     void transform_no_scramble(std::complex<T> *inout, long long batch = 1)
     {
+        if (!native) {
+            for (long long b = 0; b < batch; b++) impl->template transform<inv>((T *)(inout + b * n));
+            return;
+        }
         const size_t bytes = sizeof(std::complex<T>) * (size_t)n * batch;
         gb300::staged(inout, bytes, inout, bytes, out_, in_, [&](void *o, const void *) {
             gb300::check(gfft_fft_transform_no_scramble(gb300::dtype<T>(), n, batch, inv, o, nullptr));
@@ -141,6 +104,15 @@ struct FFT {
     template <bool inv>
     void transform(std::complex<T> *out, const std::complex<T> *in, long long batch = 1)
     {
+        if (!native) {
+            for (long long b = 0; b < batch; b++) {
+                std::complex<T> *o = out + b * n;
+                const std::complex<T> *i = in + b * n;
+                gb300::detail::scramble_by(n, [&](int r, int k) { o[r] = i[k]; });
+                impl->template transform<inv>((T *)o);
+            }
+            return;
+        }
         const size_t bytes = sizeof(std::complex<T>) * (size_t)n * batch;
         gb300::staged(out, bytes, in, bytes, out_, in_, [&](void *o, const void *i) {
             gb300::check(gfft_fft_transform(gb300::dtype<T>(), n, batch, inv, o, i, nullptr));
@@ -156,6 +128,15 @@ struct FFT {
     /// full complex spectrum of n reals (fft.h:90-94)
     void transform_real(std::complex<T> *out, const T *in, long long batch = 1)
     {
+        if (!native) {
+            for (long long b = 0; b < batch; b++) {
+                std::complex<T> *o = out + b * n;
+                const T *i = in + b * n;
+                gb300::detail::scramble_by(n, [&](int r, int k) { o[r] = std::complex<T>(i[k], T(0)); });
+                impl->template transform<false>((T *)o);
+            }
+            return;
+        }
         gb300::staged(out, sizeof(std::complex<T>) * (size_t)n * batch, in, sizeof(T) * (size_t)n * batch, out_, in_,
                       [&](void *o, const void *i) {
                           gb300::check(gfft_fft_transform_real(gb300::dtype<T>(), n, batch, o, i, nullptr));
@@ -165,6 +146,11 @@ struct FFT {
     /// FFT of in1 + i*in2; separate with separate_2x_real_FFT (fft.h:100-105)
     void transform_interleave(std::complex<T> *out, const T *in1, const T *in2)
     {
+        if (!native) {
+            gb300::detail::scramble_by(n, [&](int r, int k) { out[r] = std::complex<T>(in1[k], in2[k]); });
+            impl->template transform<false>((T *)out);
+            return;
+        }
         const bool dev = gb300::on_device(in1) && gb300::on_device(in2);
         const T *a = in1, *b = in2;
         if (!dev) {
@@ -184,18 +170,29 @@ struct FFT {
 
 private:
     int n = 0;
+    FFTImplPtr<T> impl;  // the factory's backend object (non-GB300 factories)
     gb300::Buffer in_, out_, in2_;
 };
 
 /// Column-wise FFT of `cols` columns of n rows (fft.h:115-171)
-template <class T>
+template <class T, FFTVertImplFactory<T> *factory = backend::GetVertImpl>
 struct FFTVert {
+    static constexpr bool native = factory == static_cast<FFTVertImplFactory<T> *>(&gb300::GetVertImpl<T>);
+
     FFTVert() = default;
-    explicit FFTVert(int n) : n(n) { gb300::check(n > 0 && (n & (n - 1)) == 0 ? GFFT_OK : GFFT_ERR_INVALID_SIZE); }
+    explicit FFTVert(int n) : n(n)
+    {
+        gb300::check(n > 0 && (n & (n - 1)) == 0 ? GFFT_OK : GFFT_ERR_INVALID_SIZE);
+        if (!native) impl = factory(n, T());
+    }
 
     template <bool inv>
     void transform_no_scramble(std::complex<T> *data, stride_t stride, index_t cols)
     {
+        if (!native) {
+            impl->template transform<inv>((T *)data, (int)(2 * stride), cols);
+            return;
+        }
         const size_t bytes = sizeof(std::complex<T>) * (size_t)n * stride;
         gb300::staged(data, bytes, data, bytes, out_, in_, [&](void *o, const void *) {
             gb300::check(gfft_vert_transform_no_scramble(gb300::dtype<T>(), n, inv, o, stride, cols, nullptr));
@@ -206,6 +203,14 @@ struct FFTVert {
     void transform(std::complex<T> *out, stride_t out_stride, const std::complex<T> *in, stride_t in_stride,
                    index_t cols)
     {
+        if (!native) {
+            // rows in bit-reversed order (scramble_rows, FFTUtil.h:85-98)
+            gb300::detail::scramble_by(n, [&](int r, int k) {
+                for (index_t c = 0; c < cols; c++) out[r * out_stride + c] = in[k * in_stride + c];
+            });
+            impl->template transform<inv>((T *)out, (int)(2 * out_stride), cols);
+            return;
+        }
         gb300::staged(out, sizeof(std::complex<T>) * (size_t)n * out_stride, in,
                       sizeof(std::complex<T>) * (size_t)n * in_stride, out_, in_,
                       [&](void *o, const void *i) {
@@ -225,18 +230,28 @@ struct FFTVert {
 
 private:
     int n = 0;
+    FFTVertImplPtr<T> impl;
     gb300::Buffer in_, out_;
 };
 
 /// Real-FFT adjustment of an n/2-point spectrum (fft.h:173-196)
-template <class T>
+template <class T, FFTDITImplFactory<T> *factory = backend::GetDITImpl>
 class DIT {
 public:
+    static constexpr bool native = factory == static_cast<FFTDITImplFactory<T> *>(&gb300::GetDITImpl<T>);
+
     DIT() = default;
-    explicit DIT(int n) : n(n) {}
+    explicit DIT(int n) : n(n)
+    {
+        if (!native) impl = factory(n, T());
+    }
 
     void apply(std::complex<T> *out, const std::complex<T> *in, bool half)
     {
+        if (!native) {
+            impl->apply((T *)out, (const T *)in, half);
+            return;
+        }
         const size_t in_bytes = sizeof(std::complex<T>) * (size_t)(n > 1 ? n / 2 : 1);
         const size_t out_bytes = sizeof(std::complex<T>) * (size_t)(half ? n / 2 + 1 : n);
         gb300::staged(out, out_bytes, in, in_bytes, out_, in_, [&](void *o, const void *i) {
@@ -250,6 +265,7 @@ public:
 
 private:
     int n = 0;
+    FFTDITImplPtr<T> impl;
     gb300::Buffer in_, out_;
 };
 
@@ -299,13 +315,37 @@ void separate_2x_real_FFT(std::complex<T> *out1, std::complex<T> *out2, const st
 }
 
 /// 1D FFT of real data (FFTReal.h:186-221); the output buffer holds n bins
-template <class T>
+template <class T, FFTImplFactory<T> *factory = backend::GetImpl, FFTDITImplFactory<T> *dit_factory = backend::GetDITImpl>
 struct RealFFT {
+    static constexpr bool native = factory == static_cast<FFTImplFactory<T> *>(&gb300::GetImpl<T>) &&
+                                   dit_factory == static_cast<FFTDITImplFactory<T> *>(&gb300::GetDITImpl<T>);
+
     RealFFT() = default;
-    RealFFT(int n) : n(n) {}
+    RealFFT(int n) : n(n)
+    {
+        if (!native && n > 1) {
+            impl = factory(n / 2, T());
+            dit = dit_factory(n, T());
+        }
+    }
 
     void forward(std::complex<T> *out, const T *in, bool half, long long batch = 1)
     {
+        if (!native) {
+            for (long long b = 0; b < batch; b++) {
+                std::complex<T> *o = out + b * n;
+                const T *i = in + b * n;
+                if (n == 1) {
+                    o[0] = i[0];
+                    continue;
+                }
+                // n reals as n/2 complex, bit-reversed, transformed, adjusted
+                gb300::detail::scramble_by(n / 2, [&](int r, int k) { o[r] = std::complex<T>(i[2 * k], i[2 * k + 1]); });
+                impl->forward((T *)o);
+                dit->apply((T *)o, (const T *)o, half);
+            }
+            return;
+        }
         // half mode writes n/2+1 bins per transform and leaves the rest of
         // each n-element output slot untouched, like the reference
         gb300::staged(out, sizeof(std::complex<T>) * (size_t)n * batch, in, sizeof(T) * (size_t)n * batch, out_, in_,
@@ -318,6 +358,8 @@ struct RealFFT {
 
 private:
     int n = 0;
+    FFTImplPtr<T> impl;
+    FFTDITImplPtr<T> dit;
     gb300::Buffer in_, out_;
 };
 
