@@ -89,7 +89,9 @@ def test_get_dit_impl_golden(exe, golden, oracle, tmp_path):
         z = golden[k + "/in"]
         n = 2 * z.size
         eps = oracle.fft_eps(z.dtype, n) * 1.5
-        assert close(call(exe, tmp_path, "dit_half", z, n), golden[k + "/half_generic"], eps), k
+        # the golden buffer holds the reference's n-element output; half
+        # mode writes its first n/2+1 bins
+        assert close(call(exe, tmp_path, "dit_half", z, n), golden[k + "/half_generic"][:n // 2 + 1], eps), k
         assert close(call(exe, tmp_path, "dit_full", z, n), golden[k + "/full_generic"], eps), k
 
 
