@@ -39,6 +39,11 @@ WORKLOADS = {
     "c2c_f32_1024x65536": ("c2c", "f32", 1 << 10, 0, 65536),
     "c2c_f64_4096x8192": ("c2c", "f64", 1 << 12, 0, 8192),
     "c2c_f32_4194304x32": ("c2c", "f32", 1 << 22, 0, 32),
+    # the other four-step sizes, 1 GB a batch
+    "c2c_f32_262144x512": ("c2c", "f32", 1 << 18, 0, 512),
+    "c2c_f32_524288x256": ("c2c", "f32", 1 << 19, 0, 256),
+    "c2c_f32_1048576x128": ("c2c", "f32", 1 << 20, 0, 128),
+    "c2c_f32_2097152x64": ("c2c", "f32", 1 << 21, 0, 64),
     "c2c_f64_65536x512": ("c2c", "f64", 1 << 16, 0, 512),
     "c2c_f32_65536x4096": ("c2c", "f32", 1 << 16, 0, 4096),
     "r2c_f32_1048576x64": ("r2c", "f32", 1 << 20, 0, 64),

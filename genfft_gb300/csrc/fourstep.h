@@ -40,6 +40,9 @@ struct FourStepKernel {
     size_t twa = 0, twb = 0; // Stockham table sizes (complex elements)
     void (*fill_a)(void *) = nullptr;
     void (*fill_b)(void *) = nullptr;
+    // pair-packed kernel (fourstep2.cuh): also needs a 16-byte aligned
+    // output and even output distances (two-row stores)
+    bool pair = false;
 };
 
 void fourstep_register(int dtype, int logn, const FourStepKernel &k);

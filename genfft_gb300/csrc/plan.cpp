@@ -16,6 +16,7 @@
 //   C2R  n/2 within the fused limit      one fused kernel (c2r.cu)
 //        otherwise                       pre-pass + C2C of n/2, inverse
 #include <algorithm>
+#include <cstdint>
 #include <cstdlib>
 #include <string>
 #include <vector>
@@ -101,14 +102,20 @@ void C2CCore::init(int dtype_, int logn_, long long batch_hint, int path, bool r
     tw_col = tile_table(dtype, kcol, logA, ccol);
     tw_row = tile_table(dtype, krow, logB, crow);
 
-    int nvar = 0;
-    const FourStepKernel *const *vars = fourstep_variants(dtype, logn, &nvar);
+    int nall = 0;
+    const FourStepKernel *const *all = fourstep_variants(dtype, logn, &nall);
+    // the pair-packed kernels (fourstep2.cuh) apart from the others
+    std::vector<const FourStepKernel *> plain_vars, pair_vars;
+    for (int i = 0; i < nall; i++) (all[i]->pair ? pair_vars : plain_vars).push_back(all[i]);
+    const bool want_pair = !real_rows && !pair_vars.empty() && env_ll("GFFT_FS_PAIR", 0) != 0;
+    const FourStepKernel *const *vars = want_pair ? pair_vars.data() : plain_vars.data();
+    int nvar = (int)(want_pair ? pair_vars.size() : plain_vars.size());
     // measured on GB300 (batches of 770 transforms of 2^15 .. 2^18 points,
     // 385 of 2^19, ...): the persistent kernel is the faster one for fp32
     // n = 2^16 .. 2^19; the tile launches for 2^15, for 2^20 and above, and
     // for fp64
     const bool fs_default = dtype == GFFT_F32 && logn >= 16 && logn <= 19;
-    const bool use_fs = path >= 0 ? path == 1 : env_ll("GFFT_FS", fs_default ? 1 : 0) != 0;
+    const bool use_fs = path >= 0 ? path == 1 : (want_pair || env_ll("GFFT_FS", fs_default ? 1 : 0) != 0);
     std::vector<const FourStepKernel *> dit_vars;
     if (real_rows) {
         // only the variants with a real-input version
@@ -142,6 +149,9 @@ void C2CCore::init(int dtype_, int logn_, long long batch_hint, int path, bool r
                 for (int i = 0; i < nvar; i++)
                     if (!best || vars[i]->cr > best->cr) best = vars[i];
             fs = best;
+        } else if (want_pair) {
+            // pair-packed: the first registered (GFFT_FS_NS picks another)
+            fs = vars[0];
         } else {
             // 256 compute threads (two or three CTAs per SM) with column
             // runs of 64 bytes or more, else the widest tile
@@ -245,6 +255,11 @@ bool C2CCore::run_persistent(int inverse, const void *in, void *out, long long b
         FourStepArgs a;
         a.in = static_cast<const char *>(in) + (size_t)(b0 * idist) * eb;
         a.out = static_cast<char *>(out) + (size_t)(b0 * odist) * eb;
+        // the pair-packed kernel stores two neighbouring outputs at once
+        if (fs->pair && ((((uintptr_t)a.out) & 15u) != 0 || (nb > 1 && (odist & 1) != 0))) {
+            if (b0 > 0) fail(GFFT_ERR_ALIGN, "output chunk not 16-byte aligned");
+            return false;
+        }
         // the input as [batch][A rows][B columns] of 8-byte units
         CUtensorMap map;
         if (!make_tensor_map_3d(&map, a.in, (unsigned long long)B * units, (unsigned long long)A,
