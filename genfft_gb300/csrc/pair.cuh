@@ -131,17 +131,18 @@ __device__ __forceinline__ void pdft(pcx *v)
 }
 
 // Stockham passes of one pair of 2^LOGN-point transforms held by thread t
-// of its group (the schedule of StockhamPlan<float, LOGN, 16>, whose
-// twiddle table it reads).  v[q] = pair point t + q G on entry and exit.
+// of its group (the schedule of StockhamPlan<float, LOGN, E_>, whose
+// twiddle table it reads: E_ pair points a thread).  v[q] = pair point
+// t + q G on entry and exit.
 // at(i): the pair point i slot of the group's exchange buffer; tw(p): the
 // table entry p; SYNC(): the group's barrier.  The first exchange write
 // comes before any SYNC: the caller orders it after the group's last reads
 // of the buffer.
-template <int LOGN, bool INV, typename At, typename Tw, typename Sync>
-__device__ __forceinline__ void pstockham_run(pcx (&v)[StockhamPlan<float, LOGN, 16>::E], int t, At at, Tw tw,
+template <int LOGN, int E_, bool INV, typename At, typename Tw, typename Sync>
+__device__ __forceinline__ void pstockham_run(pcx (&v)[StockhamPlan<float, LOGN, E_>::E], int t, At at, Tw tw,
                                               Sync SYNC)
 {
-    using SP = StockhamPlan<float, LOGN, 16>;
+    using SP = StockhamPlan<float, LOGN, E_>;
     constexpr int E = SP::E, G = SP::G, P = SP::P, R0 = SP::R0;
 #pragma unroll
     for (int m = 0; m < E / R0; m++) {

@@ -130,9 +130,11 @@ void C2CCore::init(int dtype_, int logn_, long long batch_hint, int path, bool r
         // GFFT_FS_NS name, else the rule below)
         fs = vars[0];
         const long long want_cc = env_ll("GFFT_FS_CC", 0), want_ns = env_ll("GFFT_FS_NS", 0);
-        if (want_cc || want_ns) {
+        const long long want_thr = env_ll("GFFT_FS_THREADS", 0);
+        if (want_cc || want_ns || want_thr) {
             for (int i = 0; i < nvar; i++)
-                if ((!want_cc || vars[i]->cc == want_cc) && (!want_ns || vars[i]->ns == want_ns)) {
+                if ((!want_cc || vars[i]->cc == want_cc) && (!want_ns || vars[i]->ns == want_ns) &&
+                    (!want_thr || vars[i]->threads == want_thr)) {
                     fs = vars[i];
                     break;
                 }

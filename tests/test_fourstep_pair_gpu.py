@@ -32,7 +32,8 @@ def _plan(G, n, batch, env):
 
 
 @pytest.mark.parametrize("logn,batch,env", [
-    (18, 7, {}), (19, 5, {}), (20, 4, {}), (21, 3, {}), (22, 3, {}), (22, 3, {"GFFT_FS_NS": 1}),
+    (18, 7, {}), (19, 5, {}), (20, 4, {}), (20, 4, {"GFFT_FS_THREADS": 576}), (21, 3, {}), (22, 3, {}),
+    (22, 3, {"GFFT_FS_NS": 1}), (22, 3, {"GFFT_FS_THREADS": 576}), (23, 2, {}),
 ])
 def test_pair_kernel_vs_fp64_and_tiles(gfft, oracle, logn, batch, env):
     import torch
@@ -56,8 +57,8 @@ def test_pair_kernel_vs_fp64_and_tiles(gfft, oracle, logn, batch, env):
     assert gfft.device_error() == 0
 
 
-@pytest.mark.parametrize("logn,batch", [(20, 9), (22, 4)])
-def test_pair_schedules_agree(gfft, logn, batch):
+@pytest.mark.parametrize("logn,batch,env0", [(20, 9, {}), (22, 4, {}), (22, 4, {"GFFT_FS_THREADS": 576})])
+def test_pair_schedules_agree(gfft, logn, batch, env0):
     import torch
     n = 1 << logn
     g = torch.Generator(device="cuda").manual_seed(100 + logn)
@@ -65,7 +66,7 @@ def test_pair_schedules_agree(gfft, logn, batch):
     outs = []
     for env in ({}, {"GFFT_FS_SLOTS": 1, "GFFT_FS_LAG": 0}, {"GFFT_FS_SLOTS": 2, "GFFT_FS_LAG": 1},
                 {"GFFT_FS_SLOTS": 4, "GFFT_FS_LAG": 2}):
-        p = _plan(gfft, n, batch, env)
+        p = _plan(gfft, n, batch, {**env0, **env})
         y = torch.empty_like(x)
         p.exec(y, x)
         torch.cuda.synchronize()
