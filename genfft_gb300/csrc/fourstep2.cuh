@@ -169,6 +169,8 @@ __global__ void __launch_bounds__(Fs2Cfg<LA, LB, E_, CT_, NS_>::THREADS, 1)
     if (threadIdx.x >= CT) {
         // ================= producer (one thread), as in k_fourstep
         if (threadIdx.x != CT) return;
+        // the input is read once: its L2 lines go first, before the ring's
+        const uint64_t in_policy = l2_policy_evict_first();
         int k = 0;
         bool failed = false;
         for (;;) {
@@ -197,7 +199,7 @@ __global__ void __launch_bounds__(Fs2Cfg<LA, LB, E_, CT_, NS_>::THREADS, 1)
                 mbar_arrive_expect_tx(&full[st], (uint32_t)(A * CC * 8));
 #pragma unroll 1
                 for (int r = 0; r < (int)A; r += Cfg::BOXR)
-                    tensor_load_3d(S + (size_t)r * CC, &map, j * CC, r, p, &full[st]);
+                    tensor_load_3d_hint(S + (size_t)r * CC, &map, j * CC, r, p, &full[st], in_policy);
             } else {
                 const long long t = p - a.lag;
                 const int slot = (int)(t % a.slots), use = (int)(t / a.slots);
@@ -322,13 +324,15 @@ __global__ void __launch_bounds__(Fs2Cfg<LA, LB, E_, CT_, NS_>::THREADS, 1)
             }
             bar_compute(CT);
             // 16-byte chunk c of the tile: row c / (CC/2), columns 2 (c % (CC/2)) + 0, 1
+            // the ring stays in L2 until its ROW items read it (and drop it)
             float2 *wsl = static_cast<float2 *>(a.ws) + (long long)slot * N + (long long)j * CC;
+            const uint64_t ring_policy = l2_policy_evict_last();
 #pragma unroll 4
             for (int c = tid; c < Cfg::STAGE / 2; c += CT) {
                 const int k1 = c / (CC / 2), h = c - k1 * (CC / 2);
                 const size_t off = (size_t)k1 * RB + (size_t)k1 * RB / 128 * 16 + (size_t)h * 16;
-                *reinterpret_cast<float4 *>(wsl + (long long)k1 * B + 2 * h) =
-                    *reinterpret_cast<const float4 *>(xch + off);
+                st_global_v4_hint(wsl + (long long)k1 * B + 2 * h, *reinterpret_cast<const float4 *>(xch + off),
+                                  ring_policy);
             }
             if (!publish(k, slot)) {
                 atomicOr(a.err, DEV_ERR_TMA_TIMEOUT);

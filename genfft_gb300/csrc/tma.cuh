@@ -95,4 +95,39 @@ __device__ __forceinline__ void tensor_load_3d(void *dst, const CUtensorMap *map
         : "memory");
 }
 
+// L2 eviction-priority policies (createpolicy) for the hinted accesses
+// below: evict_first for data read or written once, evict_last for data
+// that must stay in L2 until it is read back
+__device__ __forceinline__ uint64_t l2_policy_evict_first()
+{
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ uint64_t l2_policy_evict_last()
+{
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+
+// tensor_load_3d with an L2 cache policy
+__device__ __forceinline__ void tensor_load_3d_hint(void *dst, const CUtensorMap *map, int c0, int c1, int c2,
+                                                    uint64_t *bar, uint64_t policy)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1, {%2, "
+        "%3, %4}], [%5], %6;" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar)), "l"(policy)
+        : "memory");
+}
+
+// 16-byte global store with an L2 cache policy
+__device__ __forceinline__ void st_global_v4_hint(void *p, float4 v, uint64_t policy)
+{
+    asm volatile("st.global.L2::cache_hint.v4.f32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(p), "f"(v.x), "f"(v.y), "f"(v.z),
+                 "f"(v.w), "l"(policy)
+                 : "memory");
+}
+
 }  // namespace gfft
