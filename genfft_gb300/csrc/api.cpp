@@ -219,16 +219,16 @@ static gfft_plan_s *make_plan(const gfft_desc &in)
             break;
         case GFFT_KIND_C2C_2D:
             p->c2c.init(d.dtype, ilog2ll(d.n0), d.batch * d.n1);
-            p->col.init(d.dtype, ilog2ll(d.n1), TILE_COL_PLAIN);
+            p->col.init(d.dtype, ilog2ll(d.n1), TILE_COL_PLAIN, true, d.n0);
             p->launches = p->c2c.launches(d.batch * d.n1) + (int)p->col.launches(d.n0, d.batch);
             break;
         case GFFT_KIND_R2C_2D:
             p->r2c.init(d.dtype, ilog2ll(d.n0), 1, d.batch * d.n1);
-            p->col.init(d.dtype, ilog2ll(d.n1), half ? TILE_COL_PLAIN : TILE_COL_HERM, false);
-            p->launches = p->r2c.launches(d.batch * d.n1) + 1;
+            p->col.init(d.dtype, ilog2ll(d.n1), half ? TILE_COL_PLAIN : TILE_COL_HERM, false, d.n0 / 2 + 1);
+            p->launches = p->r2c.launches(d.batch * d.n1) + (int)p->col.launches(d.n0 / 2 + 1, d.batch);
             break;
         case GFFT_KIND_VERT:
-            p->col.init(d.dtype, ilog2ll(d.n0), bitrev ? TILE_COL_BITREV : TILE_COL_PLAIN);
+            p->col.init(d.dtype, ilog2ll(d.n0), bitrev ? TILE_COL_BITREV : TILE_COL_PLAIN, true, d.n1);
             p->launches = (int)p->col.launches(d.n1, d.batch);
             break;
         }

@@ -327,24 +327,30 @@ void C2CCore::run_stalled(const void *in, void *out, cudaStream_t st) const
 // ---------------------------------------------------------------------------
 // column FFTs
 
-void ColCore::init(int dtype_, int logl_, int variant_, bool allow_split)
+void ColCore::init(int dtype_, int logl_, int variant_, bool allow_split, long long max_cols)
 {
     dtype = dtype_;
     logl = logl_;
     variant = variant_;
-    // plain fp32 columns of 2^13 and 2^14 points run split (no one-launch
-    // tile holds them); 2^10 .. 2^12 on request (GFFT_COL_SPLIT=1): measured
-    // on GB300 for 4096 x 4096 the split column pass is no faster (2D C2C
-    // 1887 against 1899 GB/s with the one-launch 4096-point tiles)
-    const bool can_split =
-        allow_split && variant == TILE_COL_PLAIN && dtype == GFFT_F32 && logl >= 10 && logl <= 14;
-    if (can_split && (logl > 12 || env_ll("GFFT_COL_SPLIT", 0) != 0)) {
+    // Columns of up to 2^12 points run in one launch of tiles.  Longer ones
+    // (the reference's FFTVert goes to 2^23 rows, fft_impl_generic.h:281-315)
+    // run split; fp32 plain columns of 2^10 .. 2^12 also do on request
+    // (GFFT_COL_SPLIT=1): measured on GB300 for 4096 x 4096 the split column
+    // pass is no faster (2D C2C 1887 against 1899 GB/s with the one-launch
+    // 4096-point tiles)
+    constexpr int ONE_LAUNCH_MAX = 12;
+    const bool opt_split = allow_split && variant == TILE_COL_PLAIN && dtype == GFFT_F32 && logl >= 10 &&
+                           env_ll("GFFT_COL_SPLIT", 0) != 0;
+    if (logl > ONE_LAUNCH_MAX || opt_split) {
+        if (logl > 24) fail(GFFT_ERR_INVALID_SIZE, "column length above 2^24 is not supported");
+        rows_bitrev = variant == TILE_COL_BITREV;
+        herm_fill = variant == TILE_COL_HERM;
         l1 = logl / 2;
         l2 = logl - l1;
-        c1 = l1 <= 6 ? 64 : 32;
-        c2 = l2 <= 6 ? 64 : 32;
-        ka = tile_find(dtype, TILE_COL_TWB, l1, c1);
-        kb = tile_find(dtype, TILE_COL_PLAIN, l2, c2);
+        c1 = tile_widest(dtype, TILE_COL_TWB, l1, 64);
+        c2 = tile_widest(dtype, TILE_COL_PLAIN, l2, 64);
+        ka = c1 ? tile_find(dtype, TILE_COL_TWB, l1, c1) : nullptr;
+        kb = c2 ? tile_find(dtype, TILE_COL_PLAIN, l2, c2) : nullptr;
         if (!ka || !kb) fail(GFFT_ERR_UNSUPPORTED, "no split column kernels for this length");
         tw_a = tile_table(dtype, ka, l1, c1);
         tw_b = tile_table(dtype, kb, l2, c2);
@@ -353,16 +359,18 @@ void ColCore::init(int dtype_, int logl_, int variant_, bool allow_split)
         // (GFFT_COL_BAND_MB): measured on GB300 at 4096 x 4096 the launch
         // count dominates, not the scratch's L2 residency (2D C2C 1238 /
         // 1592 / 1747 / 1887 GB/s with 16 / 32 / 64 / 128 MB bands), so the
-        // default is 128 MB
+        // default is 128 MB.  A band holds at least one tile of each step
+        // and at most the columns there are.
         const long long H = 1LL << logl;
         const long long band_bytes = std::max<long long>(1, env_ll("GFFT_COL_BAND_MB", 128)) << 20;
-        band = std::max<long long>(64, (band_bytes / (H * (long long)cplx_bytes(dtype))) / 64 * 64);
+        const long long q = std::max(c1, c2);
+        band = std::max<long long>(q, (band_bytes / (H * (long long)cplx_bytes(dtype))) / q * q);
+        if (max_cols > 0) band = std::min(band, max_cols);
         ws_bytes = (size_t)(H * band) * cplx_bytes(dtype);
         check_cuda(cudaMalloc(&scratch, ws_bytes), "cudaMalloc(column scratch)");
         split = true;
         return;
     }
-    if (logl > 12) fail(GFFT_ERR_UNSUPPORTED, "column length above 2^12 is supported for fp32 plain columns only");
     c = tile_widest(dtype, variant, logl, (int)env_ll("GFFT_COL_MAXC", 16));
     if (!c) fail(GFFT_ERR_UNSUPPORTED, "no column kernel for this length");
     k = tile_find(dtype, variant, logl, c);
@@ -383,6 +391,15 @@ void ColCore::run(int inverse, const void *in, void *out, long long ncols, long 
                                   odist, tw, nullptr, nullptr, 0, 0u, st, scale),
                    "launch column FFT");
         return;
+    }
+    // rows in bit-reversed order: into natural order first (into out, or
+    // in place), then the plain split in place on out
+    if (rows_bitrev) {
+        check_cuda(launch_rows_bitrev(dtype, in, out, logl, ncols, ld_in, ld_out, batch, idist, odist, st),
+                   "launch row bit reversal");
+        in = out;
+        ld_in = ld_out;
+        idist = odist;
     }
     // Column FFT of H = H1 H2 points with rows r = H2 r1 + r2 and bins
     // k = k1 + H1 k2 (the four-step split along the column):
@@ -407,6 +424,10 @@ void ColCore::run(int inverse, const void *in, void *out, long long ncols, long 
                        "launch split column pass B");
         }
     }
+    // full-width real 2D: ncols = W/2 + 1 columns done, the rest mirrored
+    if (herm_fill)
+        check_cuda(launch_herm_fill(dtype, out, H1 * H2, 2 * (ncols - 1), ld_out, batch, odist, st),
+                   "launch Hermitian fill");
 }
 
 // ---------------------------------------------------------------------------

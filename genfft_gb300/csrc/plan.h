@@ -60,23 +60,29 @@ struct ColCore {
     int dtype = 0, logl = 0, variant = 0, c = 0;
     const TileKernel *k = nullptr;
     const void *tw = nullptr;
-    // split column FFTs (fp32, plain columns of 2^10 .. 2^14 points): each
-    // column of H = H1 * H2 points is two launches of short column FFTs per
-    // band of columns, through a scratch of one band (see ColCore::run)
-    bool split = false;
+    // split column FFTs (columns longer than one tile, 2^13 .. 2^24 points,
+    // and fp32 plain columns of 2^10 .. 2^12 on request): each column of
+    // H = H1 * H2 points is two launches of short column FFTs per band of
+    // columns, through a scratch of one band (see ColCore::run).  Bit-
+    // reversed rows first go through a row permutation pass (rows_bitrev);
+    // the full-width real 2D layout gets its mirrored half from a fill pass
+    // after the plain columns (herm_fill)
+    bool split = false, rows_bitrev = false, herm_fill = false;
     int l1 = 0, l2 = 0, c1 = 0, c2 = 0, lo_bits = 0;
     const TileKernel *ka = nullptr, *kb = nullptr;
     const void *tw_a = nullptr, *tw_b = nullptr, *tw_lo = nullptr, *tw_hi = nullptr;
     long long band = 0;  // columns per band
     void *scratch = nullptr;
     size_t ws_bytes = 0;
-    // allow_split = false keeps the one-launch tiles (real 2D, whose half-
-    // and full-width results agree bit for bit through the same tiles)
-    void init(int dtype, int logl, int variant, bool allow_split = true);
+    // allow_split = false keeps the one-launch tiles where they exist (real
+    // 2D, whose half- and full-width results agree bit for bit through the
+    // same tiles); max_cols bounds the scratch band (0 = no bound)
+    void init(int dtype, int logl, int variant, bool allow_split = true, long long max_cols = 0);
     void release();
     long long launches(long long ncols, long long batch) const
     {
-        return split ? 2 * batch * ((ncols + band - 1) / band) : 1;
+        if (!split) return 1;
+        return 2 * batch * ((ncols + band - 1) / band) + (rows_bitrev ? 1 : 0) + (herm_fill ? 1 : 0);
     }
     void run(int inverse, const void *in, void *out, long long ncols, long long ld_in, long long ld_out,
              long long batch, long long idist, long long odist, cudaStream_t st, double scale = 1.0) const;
@@ -178,6 +184,14 @@ cudaError_t launch_separate2x(int dtype, const void *in, void *o1, void *o2, lon
 cudaError_t launch_interleave(int dtype, const void *a, long long lda, const void *b, long long ldb, void *z,
                               long long ldz, long long rows, long long cols, cudaStream_t st);
 cudaError_t launch_bitrev_swap(int dtype, void *x, int logn, long long batch, long long dist, cudaStream_t st);
+
+// ---- passes around the split column FFTs (colsplit.cu) -----------------
+// rows i -> bit-reversed rows (in place: swaps; else a copy into out)
+cudaError_t launch_rows_bitrev(int dtype, const void *in, void *out, int logh, long long ncols, long long ld_in,
+                               long long ld_out, long long batch, long long idist, long long odist, cudaStream_t st);
+// full-width real 2D: columns W/2+1 .. W-1 from the conjugate mirror
+cudaError_t launch_herm_fill(int dtype, void *out, long long H, long long W, long long ld, long long batch,
+                             long long odist, cudaStream_t st);
 
 // ---- ragged batches (ragged.cu) ------------------------------------------
 struct RaggedPlan;

@@ -50,8 +50,9 @@ typedef enum gfft_dtype { GFFT_F32 = 0, GFFT_F64 = 1 } gfft_dtype;
 typedef enum gfft_kind {
     GFFT_KIND_C2C = 0,     /* batched 1D complex, FFT<T> (fft.h:56-113) */
     GFFT_KIND_R2C = 1,     /* batched 1D real input, RealFFT<T> (FFTReal.h:186-221) */
-    /* column lengths (2D heights, FFTVert rows) up to 2^12, and for fp32
-     * complex columns (C2C_2D, VERT without bit-reversed rows) up to 2^14 */
+    /* column lengths (2D heights, FFTVert rows) up to 2^24: up to 2^12 in
+     * one launch of column tiles, above that as two launches of shorter
+     * column FFTs per band of columns through a plan-owned scratch */
     GFFT_KIND_C2C_2D = 2,  /* 2D complex, FFT2D<T> (fft.h:198-245) */
     GFFT_KIND_R2C_2D = 3,  /* 2D real input, RealFFT2D<T> (FFTReal.h:69-184) */
     GFFT_KIND_VERT = 4     /* column FFT, FFTVert<T> (fft.h:115-171) */

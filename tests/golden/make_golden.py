@@ -127,6 +127,30 @@ def main() -> None:
         data[f"r2d2x_f32_{W}x{H}/in2"] = b
         data[f"r2d2x_f32_{W}x{H}/fwd_generic"] = gen.real_fft2d_2x(a, b)
 
+    # Columns longer than one tile (2^13 .. 2^16 rows, odd column counts):
+    # FFTVert<T> (fft.h:145-150) and the 2D transforms with tall images
+    # (FFT2D fft.h:213-218, RealFFT2D FFTReal.h:83-104).  Appended last so
+    # the draws above are unchanged; the largest cases keep the forward only.
+    for n, cols, dt, tag, inv in ((8192, 3, np.complex64, "f32", True), (16384, 3, np.complex64, "f32", False),
+                                  (65536, 1, np.complex64, "f32", False), (8192, 3, np.complex128, "f64", True),
+                                  (16384, 1, np.complex128, "f64", False)):
+        x = cplx((n, cols), dt)
+        k = f"vertlong_{tag}_{n}x{cols}"
+        data[k + "/in"] = x
+        data[k + "/fwd_generic"] = gen.fft_vert(x, False)
+        if inv:
+            data[k + "/inv_generic"] = gen.fft_vert(x, True)
+    for W, H, dt, tag in ((4, 8192, np.complex64, "f32"), (2, 8192, np.complex128, "f64")):
+        x = cplx((H, W), dt)
+        k = f"c2dlong_{tag}_{W}x{H}"
+        data[k + "/in"] = x
+        data[k + "/fwd_generic"] = gen.fft2d(x, False)
+    for W, H, rdt, tag in ((4, 8192, np.float32, "f32"), (4, 8192, np.float64, "f64")):
+        x = rng.uniform(-1, 1, (H, W)).astype(rdt)
+        k = f"r2dlong_{tag}_{W}x{H}"
+        data[k + "/in"] = x
+        data[k + "/fwd_generic"] = gen.real_fft2d(x)
+
     np.savez_compressed(OUT, **data)
     total = sum(v.nbytes for v in data.values())
     print(f"wrote {OUT}: {len(data)} arrays, {total / 1e6:.2f} MB raw")

@@ -111,6 +111,23 @@ def test_2d_bit_exact(golden, oracle):
         assert same_bits(got, golden[k + "/fwd_generic"]), k
 
 
+def test_long_columns_bit_exact(golden, oracle):
+    """Columns longer than one GPU tile (2^13 .. 2^16 rows): FFTVert and
+    tall 2D images, bit for bit against the reference's generic backend."""
+    o = oracle.Impl("oracle")
+    cases = keys(golden, "vertlong_")
+    assert len(cases) >= 5
+    for k in cases:
+        x = golden[k + "/in"]
+        assert same_bits(o.fft_vert(x, False), golden[k + "/fwd_generic"]), k
+        if k + "/inv_generic" in golden.files:
+            assert same_bits(o.fft_vert(x, True), golden[k + "/inv_generic"]), k
+    for k in keys(golden, "c2dlong_"):
+        assert same_bits(o.fft2d(golden[k + "/in"], False), golden[k + "/fwd_generic"]), k
+    for k in keys(golden, "r2dlong_"):
+        assert same_bits(o.real_fft2d(golden[k + "/in"]), golden[k + "/fwd_generic"]), k
+
+
 def test_2d_vs_dft(golden, oracle):
     """2D and real-2D are not covered by the reference's own tests; check the
     golden outputs against separable FP64 DFTs."""
