@@ -101,3 +101,24 @@ def test_tc_adjoint_is_conjugate_direction(gfft):
     torch.cuda.synchronize()
     exact = np.fft.ifft(g.astype(np.complex128)) * n
     assert rel_rms(out.cpu().numpy(), exact) <= bound(n)
+
+
+@pytest.mark.parametrize("n,batch", [(256, 64), (4096, 16), (65536, 4)])
+def test_tc_equal_error(gfft, n, batch):
+    """The split-precision path against the plain fp32 path's FP64-oracle
+    error on the same log-uniform inputs.  BF16 hi+mid+lo matches it (at
+    most 1.05x).  FP16 hi+lo does not: its 22 bits of mantissa leave about
+    1.7x the plain error (2.4e-7 against 1.5e-7 at 2^16); the test holds it
+    under 2x so that a regression shows."""
+    rng = np.random.default_rng(500 + n)
+    x = logmag(rng, (batch, n))
+    x64 = x.astype(np.complex128)
+    for inv in (False, True):
+        exact = np.fft.ifft(x64) * n if inv else np.fft.fft(x64)
+        e_plain = rel_rms(run(gfft, x, n, 0, inv), exact)
+        e_bf16 = rel_rms(run(gfft, x, n, MODES["bf16"], inv), exact)
+        e_fp16 = rel_rms(run(gfft, x, n, MODES["fp16"], inv), exact)
+        print(f"n={n} inv={inv}: plain {e_plain:.3g} bf16 {e_bf16:.3g} ({e_bf16 / e_plain:.2f}x) "
+              f"fp16 {e_fp16:.3g} ({e_fp16 / e_plain:.2f}x)")
+        assert e_bf16 <= 1.05 * e_plain, (n, inv, e_bf16, e_plain)
+        assert e_fp16 <= 2.0 * e_plain, (n, inv, e_fp16, e_plain)
