@@ -182,32 +182,6 @@ void C2CCore::init(int dtype_, int logn_, long long batch_hint, int path, bool r
         algo = 3;
         return;
     }
-    if (path < 0 && !real_rows && dtype == GFFT_F32 && logn >= 20 && env_ll("GFFT_3PASS", 0) != 0) {
-        // three passes of short tiles, N = A * C * D: A-point columns (stride
-        // C D), C-point columns inside each C x D block, D-point rows with
-        // the transposed store; the two intermediates of a group stay in L2
-        l3a = 7;
-        l3d = 7;
-        l3c = logn - 14;
-        c3a = tile_widest(dtype, TILE_COL_TW4, l3a, 16);
-        c3c = tile_widest(dtype, TILE_COL_TW4, l3c, 16);
-        c3d = tile_widest(dtype, TILE_ROW_XPOSE, l3d, 16);
-        k3a = c3a ? tile_find(dtype, TILE_COL_TW4, l3a, c3a) : nullptr;
-        k3c = c3c ? tile_find(dtype, TILE_COL_TW4, l3c, c3c) : nullptr;
-        k3d = c3d ? tile_find(dtype, TILE_ROW_XPOSE, l3d, c3d) : nullptr;
-        if (k3a && k3c && k3d) {
-            tw3a = tile_table(dtype, k3a, l3a, c3a);
-            tw3c = tile_table(dtype, k3c, l3c, c3c);
-            tw3d = tile_table(dtype, k3d, l3d, c3d);
-            wn_tables(dtype, logn - l3a, &lo_bits_b, &tw_lo_b, &tw_hi_b);
-            group = std::max<long long>(1, std::min<long long>(env_ll("GFFT_3PASS_GROUP", 1), batch_hint));
-            ws_bytes = 2 * (size_t)(group * N) * cplx_bytes(dtype);
-            check_cuda(cudaMalloc(&ws, ws_bytes / 2), "cudaMalloc(workspace)");
-            check_cuda(cudaMalloc(&ws2, ws_bytes / 2), "cudaMalloc(workspace)");
-            algo = 4;
-            return;
-        }
-    }
     // transforms per launch pair, bounded by the workspace budget: fewer,
     // larger launch pairs (measured on GB300, 1 GB against 512 MB: +2 % for
     // n = 2^20 .. 2^23, e.g. 2^22 x 32 in one pair instead of two)
@@ -222,9 +196,8 @@ void C2CCore::init(int dtype_, int logn_, long long batch_hint, int path, bool r
 void C2CCore::release()
 {
     if (ws) cudaFree(ws);
-    if (ws2) cudaFree(ws2);
     if (fs_ctr) cudaFree(fs_ctr);
-    ws = ws2 = nullptr;
+    ws = nullptr;
     fs_ctr = nullptr;
 }
 
@@ -241,7 +214,6 @@ int C2CCore::launches(long long batch) const
         const long long chunk = fs_chunk(fs->nc + fs_nr, fs_lag);
         return (int)((batch + chunk - 1) / chunk);
     }
-    if (algo == 4) return 2 * (int)((batch + group - 1) / group) + (int)batch;
     return 2 * (int)((batch + group - 1) / group);
 }
 
@@ -256,35 +228,8 @@ void C2CCore::run(int inverse, const void *in, void *out, long long batch, long 
     if (istride != 1 || ostride != 1)
         fail(GFFT_ERR_UNSUPPORTED, "lengths above the fused limit need unit element strides");
     if (algo == 3 && !fs_real && run_persistent(inverse, in, out, batch, idist, odist, st, scale)) return;
-    const size_t eb = cplx_bytes(dtype);
-    if (algo == 4) {
-        // N = A B, B = C D; input x[b + B a], b = d + D c; output
-        // X[k1 + A (kc + C kd)]:
-        //   1: for every b, an A-point FFT over a (stride B) times W_N^(b k1)
-        //      -> Y[k1 B + b]                                 (column tiles)
-        //   2: for every (k1, d), a C-point FFT over c (stride D) times
-        //      W_B^(d kc) -> Z[k1 B + kc D + d]                (column tiles)
-        //   3: for every (k1, kc), a D-point FFT over d, stored at
-        //      X[k1 + A kc + A C kd]                  (row tiles, transposed)
-        const long long A = 1LL << l3a, C = 1LL << l3c, D = 1LL << l3d, B = C * D, N = A * B;
-        for (long long g0 = 0; g0 < batch; g0 += group) {
-            const long long nb = std::min(group, batch - g0);
-            const char *src = static_cast<const char *>(in) + (size_t)(g0 * idist) * eb;
-            char *dst = static_cast<char *>(out) + (size_t)(g0 * odist) * eb;
-            check_cuda(launch_colpass(*k3a, inverse, B / c3a, nb, src, ws, B, B, B, idist, N, tw3a, tw_lo, tw_hi,
-                                      lo_bits, (unsigned)(N - 1), st),
-                       "launch three-pass step 1");
-            check_cuda(launch_colpass(*k3c, inverse, D / c3c, nb * A, ws, ws2, D, D, D, B, B, tw3c, tw_lo_b, tw_hi_b,
-                                      lo_bits_b, (unsigned)(B - 1), st),
-                       "launch three-pass step 2");
-            for (long long t = 0; t < nb; t++)
-                check_cuda(launch_rowpass(*k3d, inverse, A / c3d, C, static_cast<const char *>(ws2) + (size_t)(t * N) * eb,
-                                          dst + (size_t)(t * odist) * eb, A, B, A * C, D, A, tw3d, st, scale),
-                           "launch three-pass step 3");
-        }
-        return;
-    }
     const long long A = 1LL << logA, B = 1LL << logB, N = A * B;
+    const size_t eb = cplx_bytes(dtype);
     const unsigned nmask = (unsigned)(N - 1);
     for (long long g0 = 0; g0 < batch; g0 += group) {
         const long long nb = std::min(group, batch - g0);

@@ -20,7 +20,7 @@ bool is_pow2(long long n);
 // memory limit, else the four-step column + row passes through a workspace.
 struct C2CCore {
     int dtype = 0, logn = 0;
-    int algo = 0;  // 1 fused, 2 four-step tile launches, 3 persistent four-step, 4 three-pass tiles
+    int algo = 0;  // 1 fused, 2 four-step tile launches, 3 persistent four-step
     const void *tw = nullptr;
     // persistent four-step: kernel, ring of `fs_slots` transforms, counters
     const FourStepKernel *fs = nullptr;
@@ -33,14 +33,8 @@ struct C2CCore {
     const TileKernel *kcol = nullptr, *krow = nullptr;
     const void *tw_col = nullptr, *tw_row = nullptr, *tw_lo = nullptr, *tw_hi = nullptr;
     long long group = 0;       // transforms per column/row launch pair
-    void *ws = nullptr;        // group * n (algo 2, 4) or fs_slots * n (algo 3) elements
+    void *ws = nullptr;        // group * n (algo 2) or fs_slots * n (algo 3) elements
     size_t ws_bytes = 0;
-    // three-pass split (algo 4, fp32 n = 2^20 .. 2^24): N = A * C * D with
-    // A = D = 2^7 and C = N / 2^14, short tiles throughout (see C2CCore::run)
-    int l3a = 0, l3c = 0, l3d = 0, c3a = 0, c3c = 0, c3d = 0, lo_bits_b = 0;
-    const TileKernel *k3a = nullptr, *k3c = nullptr, *k3d = nullptr;
-    const void *tw3a = nullptr, *tw3c = nullptr, *tw3d = nullptr, *tw_lo_b = nullptr, *tw_hi_b = nullptr;
-    void *ws2 = nullptr;       // group * n elements
 
     // path: -1 the measured default (or GFFT_FS), 1 the persistent
     // four-step kernel, 0 the tile launches.  real_rows (with path 1): a
