@@ -40,6 +40,7 @@ WORKLOADS = {
     "c2c_f64_4096x8192": ("c2c", "f64", 1 << 12, 0, 8192),
     "c2c_f32_4194304x32": ("c2c", "f32", 1 << 22, 0, 32),
     # the other four-step sizes, 1 GB a batch
+    "c2c_f32_131072x1024": ("c2c", "f32", 1 << 17, 0, 1024),
     "c2c_f32_262144x512": ("c2c", "f32", 1 << 18, 0, 512),
     "c2c_f32_524288x256": ("c2c", "f32", 1 << 19, 0, 256),
     "c2c_f32_1048576x128": ("c2c", "f32", 1 << 20, 0, 128),

@@ -14,9 +14,10 @@
 //     two adjacent rows of a ROW item, so the butterflies, rotations and
 //     twiddle products of two transforms issue as one packed instruction;
 //   * each pair of sub-transforms exchanges through its own padded buffer,
-//     separate from the stage, so a warp hands the stage back to the
-//     producer as soon as it has read its points and the next item's copy
-//     overlaps the whole transform of this one;
+//     separate from the stage, under its own barrier (__syncwarp where the
+//     pair is one warp's), so a warp hands the stage back to the producer
+//     as soon as it has read its points and the next item's copy overlaps
+//     the whole transform of this one;
 //   * both epilogues go through shared memory so that every store writes
 //     whole 32-byte sectors: a COL item writes CC * 8 contiguous bytes of
 //     each ring row, a ROW item CR * 8 contiguous bytes of each output run
@@ -70,13 +71,30 @@ struct Fs2Cfg {
     static constexpr bool TAB_SMEM = TAB_OFF + TAB_BYTES + BAR_BYTES <= 227 * 1024;
     static constexpr size_t BAR_OFF = (TAB_OFF + (TAB_SMEM ? TAB_BYTES : 0) + 15) / 16 * 16;
     static constexpr size_t SMEM = BAR_OFF + BAR_BYTES;
+    // a pair unit of one warp exchanges under __syncwarp; longer units use
+    // named barriers 2 .. 2 + units - 1 (1 is the compute warps' barrier)
+    static constexpr bool SYNC_FITS = (GA == 32 || (GA % 32 == 0 && UA <= 14)) && (GB == 32 || (GB % 32 == 0 && UB <= 14));
     static constexpr bool FITS = SMEM <= 227 * 1024 && CT % 32 == 0 && CT % GA == 0 && CT % GB == 0 && UA >= 1 &&
                                  UB >= 1 && CC <= 16 && CR <= 16 && B % CC == 0 && A % CR == 0 && A % BOXR == 0 &&
-                                 EPI_FITS;
+                                 EPI_FITS && SYNC_FITS;
+    // two CTAs an SM where their shared memory fits (8 pair points a
+    // thread keep the registers within half the file)
+    static constexpr int MIN_BLOCKS = (E <= 8 && THREADS <= 320 && 2 * (SMEM + 1024) <= 228 * 1024) ? 2 : 1;
 };
 
+// named barrier `id` over `n` threads
+__device__ __forceinline__ void bar_named(int id, int n) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory"); }
+
+// the exchange barrier of pair unit u (G threads)
+template <int G>
+__device__ __forceinline__ void unit_sync(int u)
+{
+    if constexpr (G == 32) __syncwarp();
+    else bar_named(2 + u, G);
+}
+
 template <int LA, int LB, int E_, int CT_, int NS_, bool INV>
-__global__ void __launch_bounds__(Fs2Cfg<LA, LB, E_, CT_, NS_>::THREADS, 1)
+__global__ void __launch_bounds__(Fs2Cfg<LA, LB, E_, CT_, NS_>::THREADS, Fs2Cfg<LA, LB, E_, CT_, NS_>::MIN_BLOCKS)
     k_fs2(const __grid_constant__ CUtensorMap map, const FourStepArgs a)
 {
     using Cfg = Fs2Cfg<LA, LB, E_, CT_, NS_>;
@@ -303,7 +321,7 @@ __global__ void __launch_bounds__(Fs2Cfg<LA, LB, E_, CT_, NS_>::THREADS, 1)
             if (lane == 0) mbar_arrive(&empty[st]);
             pcx *my = reinterpret_cast<pcx *>(xch) + (size_t)u * Cfg::XA;
             pstockham_run<LA, E, INV>(
-                v, tt, [my](int i) -> pcx & { return my[ppad(i)]; }, tw_a, []() { bar_compute(CT); });
+                v, tt, [my](int i) -> pcx & { return my[ppad(i)]; }, tw_a, [u]() { unit_sync<GA>(u); });
             // W_N^(col k1) twiddle, then the tile through shared memory:
             // row k1 holds the item's CC columns (CC * 8 bytes)
             const unsigned col = (unsigned)(j * CC + 2 * u);
@@ -357,7 +375,7 @@ __global__ void __launch_bounds__(Fs2Cfg<LA, LB, E_, CT_, NS_>::THREADS, 1)
             if (lane == 0) mbar_arrive(&empty[st]);
             pcx *my = reinterpret_cast<pcx *>(xch) + (size_t)u * Cfg::XB;
             pstockham_run<LB, E, INV>(
-                v, tt, [my](int i) -> pcx & { return my[ppad(i)]; }, tw_b, []() { bar_compute(CT); });
+                v, tt, [my](int i) -> pcx & { return my[ppad(i)]; }, tw_b, [u]() { unit_sync<GB>(u); });
             // through shared memory: row k2 holds the item's CR rows k1
             constexpr int RB = CR * 8;
             const bool scaled = scale != 1.0f;

@@ -1,5 +1,5 @@
 // fourstep2_f32.cu -- registrations of the pair-packed persistent four-step
-// kernel (fourstep2.cuh), fp32 n = 2^18 .. 2^23.  R(logn, E, CT, NS): E
+// kernel (fourstep2.cuh), fp32 n = 2^16 .. 2^23.  R(logn, E, CT, NS): E
 // pair points a thread, CT compute threads, NS shared-memory stages.
 #include "fourstep2.cuh"
 #include "fourstep_impl.cuh"
@@ -42,9 +42,10 @@ struct Fs2Reg {
 #endif
 #define R(L, E, C, S) static Fs2Reg<L, E, C, S> fs2_f32_##L##_##E##_##C##_##S;
 #if FS2_SET == 0
-R(22, 16, 256, 2) R(22, 16, 256, 1) R(22, 8, 512, 1) R(23, 16, 256, 1)
+R(22, 16, 256, 2) R(22, 16, 256, 1) R(22, 8, 512, 1) R(23, 16, 256, 1) R(16, 8, 256, 2) R(17, 8, 256, 2)
 #else
-R(18, 16, 256, 2) R(19, 16, 256, 2) R(20, 16, 256, 2) R(20, 8, 512, 1) R(21, 16, 256, 2)
+R(18, 16, 256, 2) R(18, 8, 256, 2) R(19, 16, 256, 2) R(19, 8, 256, 2) R(20, 16, 256, 2) R(20, 8, 512, 1)
+R(20, 8, 256, 2) R(21, 16, 256, 2)
 #endif
 #undef R
 }  // namespace gfft

@@ -1,6 +1,6 @@
 """The pair-packed persistent four-step kernel (fourstep2.cuh: two
 sub-transforms per thread on packed FP32 instructions) for fp32
-n = 2^18 .. 2^22: against an FP64 transform at the fp32 bound
+n = 2^16 .. 2^23: against an FP64 transform at the fp32 bound
 2e-7*log2(n), against the two-launch tile path, under several ring
 schedules (which must agree bit for bit), in place, with the in-kernel
 scale, with an output too misaligned for its 16-byte stores (the plan then
@@ -32,7 +32,8 @@ def _plan(G, n, batch, env):
 
 
 @pytest.mark.parametrize("logn,batch,env", [
-    (18, 7, {}), (19, 5, {}), (20, 4, {}), (20, 4, {"GFFT_FS_THREADS": 576}), (21, 3, {}), (22, 3, {}),
+    (16, 9, {}), (17, 7, {}), (18, 7, {}), (18, 7, {"GFFT_FS_CC": 8}), (19, 5, {}), (19, 5, {"GFFT_FS_CC": 8}),
+    (20, 4, {}), (20, 4, {"GFFT_FS_THREADS": 576}), (20, 4, {"GFFT_FS_CC": 4}), (21, 3, {}), (22, 3, {}),
     (22, 3, {"GFFT_FS_NS": 1}), (22, 3, {"GFFT_FS_THREADS": 576}), (23, 2, {}),
 ])
 def test_pair_kernel_vs_fp64_and_tiles(gfft, oracle, logn, batch, env):
@@ -57,7 +58,8 @@ def test_pair_kernel_vs_fp64_and_tiles(gfft, oracle, logn, batch, env):
     assert gfft.device_error() == 0
 
 
-@pytest.mark.parametrize("logn,batch,env0", [(20, 9, {}), (22, 4, {}), (22, 4, {"GFFT_FS_THREADS": 576})])
+@pytest.mark.parametrize("logn,batch,env0", [(16, 37, {}), (20, 9, {}), (22, 4, {}),
+                                          (22, 4, {"GFFT_FS_THREADS": 576})])
 def test_pair_schedules_agree(gfft, logn, batch, env0):
     import torch
     n = 1 << logn
