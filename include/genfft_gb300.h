@@ -120,6 +120,10 @@ gfft_status gfft_exec_adjoint(gfft_plan plan, int inverse, void *out, const void
 /* Same transform on HOST buffers (the reference's calling convention):
  * copies in, transforms and copies out in pipelined chunks, synchronously.
  * Pinned host memory gives full link bandwidth; pageable memory works.
+ * Single-kernel C2C sizes (see gfft_max_fused_size) on pinned buffers, on a
+ * device that reads host memory through the host's page tables (GB300 with
+ * Grace), skip the staging: the kernel reads the input and writes the
+ * output over the host link itself (GFFT_HOST_DIRECT=0 turns this off).
  * Whole transforms are staged, so each must lie inside its own idist /
  * odist block (GFFT_ERR_UNSUPPORTED for batch-interleaved layouts, which
  * run on device buffers). */

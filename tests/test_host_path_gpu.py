@@ -85,3 +85,32 @@ def test_host_rejects_interleaved_batches(gfft):
     with pytest.raises(gfft.GFFTError) as e:
         p.exec_host_ptr(hy.ctypes.data, hx.ctypes.data)
     assert e.value.name == "GFFT_ERR_UNSUPPORTED"
+
+
+@pytest.mark.parametrize("logn,batch", [(12, 300), (10, 1000), (14, 17)])
+def test_host_c2c_pinned_direct(gfft, logn, batch):
+    """Single-kernel C2C on pinned host buffers (the path where the kernel
+    reads and writes host memory itself, on a device that sees host page
+    tables): bit for bit the device exec, guard regions of the pinned
+    output intact, in place too."""
+    import torch
+    n = 1 << logn
+    x = torch.randn(batch, n, dtype=torch.complex64, device="cuda")
+    p = gfft.Plan(gfft.KIND_C2C, gfft.F32, n, 0, batch)
+    hx = x.cpu().pin_memory()
+    g = GUARD // 8
+    for inv in (False, True):
+        y = torch.empty_like(x)
+        p.exec(y, x, inv)
+        torch.cuda.synchronize()
+        hbuf = torch.full((batch * n + 2 * g,), complex(float("nan"), float("nan")), dtype=torch.complex64)
+        hbuf = hbuf.pin_memory()
+        hbuf[:g] = 7 + 7j
+        hbuf[g + batch * n:] = 7 + 7j
+        out = hbuf[g:g + batch * n]
+        p.exec_host_ptr(out.data_ptr(), hx.data_ptr(), inv)
+        assert torch.equal(out.view(batch, n), y.cpu()), inv
+        assert torch.all(hbuf[:g] == 7 + 7j) and torch.all(hbuf[g + batch * n:] == 7 + 7j)
+        hi = hx.clone().pin_memory()
+        p.exec_host_ptr(hi.data_ptr(), hi.data_ptr(), inv)
+        assert torch.equal(hi, y.cpu()), inv
