@@ -846,7 +846,9 @@ def run_ours(args):
                          "avg_launch_ms": round(avg_launch_ms, 5),
                          "algorithmic_bytes_per_exec": batch * per_transform},
             "e2e": {"value": round(e2e_gbs, 2), "unit": "GB/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h, "api": "gfft_exec_host (pinned host buffers)",
+                    "d2h_bytes_per_step": d2h,
+                    "api": "gfft_exec_host (pinned host buffers; single-kernel C2C reads and writes them over the "
+                           "host link directly, other plans stage chunks through device memory)",
                     "steps": e2e_steps},
             "gpu_launches": E * K * launches_per_exec,
             "check": check, "e2e_check": e2e_check, "accuracy": accuracy,
