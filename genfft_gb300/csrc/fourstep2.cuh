@@ -1,6 +1,7 @@
 // fourstep2.cuh -- the persistent four-step C2C (fourstep.cuh) with two
 // sub-transforms per thread on packed FP32 instructions (pair.cuh), for
-// fp32 n = A * B with A, B = 2^9 .. 2^12.
+// fp32 n = A * B with A, B = 2^8 .. 2^12.  Opt-in (GFFT_FS_PAIR=1):
+// measured on GB300 it is slower than the default paths except at 2^18.
 //
 // Same split, schedule and intermediate ring as k_fourstep: COL items (CC
 // columns of A points of transform p: HBM -> FFT -> W_N twiddle -> ring
@@ -25,7 +26,11 @@
 //   * the compute warps never fence: a publisher warp takes each finished
 //     item (mbarrier hand-off, release / acquire within the CTA), makes it
 //     visible to the GPU and counts it, so the item's stores drain while
-//     the compute warps start the next one.
+//     the compute warps start the next one;
+//   * L2 policies keep the ring resident: the input's tensor copies are
+//     evict-first, the ring's stores evict-last;
+//   * variants of 8 pair points a thread and up to about 113 KB of shared
+//     memory run two CTAs an SM.
 // Accounting: col_done[slot] and row_done[slot] count COL and ROW items, as
 // in k_fourstep; a ROW item is counted once its rows are in shared memory
 // (and their L2 lines dropped), a COL item once its stores are visible.
