@@ -9,7 +9,6 @@
 // (fp64) passes exchange through padded shared memory, and the last pass
 // stores straight to global memory.  Roofline: HBM-bound, 2 * N * 2 *
 // sizeof(T) algorithmic bytes per transform.
-#include <cstdlib>
 #include <mutex>
 
 #include "internal.h"
@@ -62,10 +61,6 @@ __global__ void __launch_bounds__(FusedCfg<T, LOGN>::THREADS, FusedCfg<T, LOGN>:
     const long long b = (long long)blockIdx.x * Cfg::TPC + g;
     const bool active = b < batch;
 
-    // launched as a programmatic dependent of the previous kernel on the
-    // stream: wait for that grid's completion (and its writes) before the
-    // first read; a no-op in an ordinary launch
-    asm volatile("griddepcontrol.wait;" ::: "memory");
     cpx<T> v[E];
     if (active) {
         const cpx<T> *src = in + b * idist + (long long)t * istride;
@@ -78,10 +73,6 @@ __global__ void __launch_bounds__(FusedCfg<T, LOGN>::THREADS, FusedCfg<T, LOGN>:
     cpx<T> *my = sm + g * SP::SMEM;
     stockham_run<T, LOGN, FusedE<T>::value, INV>(
         v, t, [my](int i) -> cpx<T> & { return my[spad<T>(i)]; }, tw, []() { __syncthreads(); });
-    // this CTA's reads are done: the next kernel on the stream may start
-    // launching once every CTA of this grid got here (it still waits for
-    // this grid's completion before it reads)
-    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     if (active) {
         cpx<T> *dst = out + b * odist + (long long)t * ostride;
 #pragma unroll
@@ -174,25 +165,7 @@ cudaError_t launch_fused_c2c(int dtype, int logn, int inverse, const FusedC2CArg
     void *args[] = {(void *)&in,      (void *)&out,     (void *)&batch, (void *)&idist, (void *)&odist,
                     (void *)&istride, (void *)&ostride, (void *)&tw,
                     dtype == GFFT_F32 ? (void *)&scale_f : (void *)&scale_d};
-    // programmatic dependent launch (GFFT_PDL, default on): this grid may be
-    // launched while the previous kernel on the stream finishes its last
-    // wave; the kernel waits for it before reading
-    static const bool pdl = [] {
-        const char *v = std::getenv("GFFT_PDL");
-        return !(v && *v == '0');
-    }();
-    if (!pdl) return cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(e.threads), args, e.smem, st);
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)grid);
-    cfg.blockDim = dim3(e.threads);
-    cfg.dynamicSmemBytes = e.smem;
-    cfg.stream = st;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    return cudaLaunchKernelExC(&cfg, fn, args);
+    return cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(e.threads), args, e.smem, st);
 }
 
 }  // namespace gfft
