@@ -17,14 +17,10 @@
 
 namespace gfft {
 
-// points per thread: radix-16 registers for fp32 and fp64 (GFFT_FUSED_E64=8
-// at build time restores radix-8 for fp64)
-#ifndef GFFT_FUSED_E64
-#define GFFT_FUSED_E64 16
-#endif
+// points per thread: radix-16 registers for fp32, radix-8 for fp64
 template <typename T>
 struct FusedE {
-    static constexpr int value = sizeof(T) == 4 ? 16 : GFFT_FUSED_E64;
+    static constexpr int value = sizeof(T) == 4 ? 16 : 8;
 };
 
 template <typename T>
@@ -44,11 +40,7 @@ struct FusedCfg {
     // (fp32 n = 2^12 and n <= 2^8, ptxas -v), else three for CTAs of up to
     // 256 threads (the residency the compiler picked unconstrained) and two
     // for 512-thread CTAs
-    // fp64 with 16 points a thread: two 256-thread CTAs (128 registers), one
-    // of 512
-    static constexpr bool WIDE64 = sizeof(T) == 8 && FusedE<T>::value == 16 && LOGN >= 5;
-    static constexpr int MIN_BLOCKS = WIDE64 ? (THREADS <= 256 ? 2 : 1)
-                                    : (sizeof(T) == 4 && (LOGN == 12 || (LOGN >= 5 && LOGN <= 8))) ? 4
+    static constexpr int MIN_BLOCKS = (sizeof(T) == 4 && (LOGN == 12 || (LOGN >= 5 && LOGN <= 8))) ? 4
                                     : THREADS <= 256 ? 3 : THREADS <= 512 ? 2 : 1;
 };
 
