@@ -15,8 +15,10 @@ exactly K steps, barrier + synchronize on both sides, max over ranks);
 `e2e` is the same metric through the C ABI's host-buffer call
 (gfft_exec_host) with the H2D and D2H copies inside the timed region.
 
-Multi-GPU (torchrun): every rank runs its own copy of the batch (the batch
-shards with no exchange), so scaling is weak and value sums all ranks.
+Multi-GPU (torchrun): the global batch is the workload's batch times the
+number of ranks, split into contiguous shards (genfft_gb300.shard) with no
+exchange between ranks; each rank transforms its own shard, so scaling is
+weak and value sums all ranks.
 """
 from __future__ import annotations
 
@@ -441,12 +443,14 @@ def kernel_name(G, kind, dtype, n0, mode=0, launches=1):
     return "plan kernels"
 
 
-def make_case(G, torch, kind, dtype, n0, n1, batch, rank, mode=0):
-    """Inputs, outputs, plan and the per-step exec list for one workload."""
+def make_case(G, torch, kind, dtype, n0, n1, batch, first, mode=0):
+    """Inputs, outputs, plan and the per-step exec list for one workload
+    (`first`: the index of this shard's first transform in the global
+    batch, which seeds its inputs)."""
     rdt = torch.float32 if dtype == "f32" else torch.float64
     cdt = torch.complex64 if dtype == "f32" else torch.complex128
     dcode = G.F32 if dtype == "f32" else G.F64
-    gen = torch.Generator(device="cuda").manual_seed(1234 + rank)
+    gen = torch.Generator(device="cuda").manual_seed(1234 + first)
     if kind == "c2c" and mode:
         # tensor-core workload: magnitudes log-uniform in [1e-3, 1e3], uniform phase
         shape_in = shape_out = (batch, n0)
@@ -731,7 +735,10 @@ def run_ours(args):
     torch.cuda.set_device(dev)
     kind, dtype, n0, n1, batch, mode = workload(args.workload)
     G.lib()
-    x, y, z, plan, execs = make_case(G, torch, kind, dtype, n0, n1, batch, rank, mode)
+    # this rank's shard of the global batch (batch transforms per rank)
+    from genfft_gb300.shard import shard_range
+    first, batch = shard_range(batch * world, rank, world)
+    x, y, z, plan, execs = make_case(G, torch, kind, dtype, n0, n1, batch, first, mode)
     # launches of one exec in the direction(s) the step runs
     launches_per_exec = sum(plan.launches(inv) for _, _, inv in execs) // len(execs)
     stream = torch.cuda.current_stream()
@@ -834,7 +841,8 @@ def run_ours(args):
                        "layout": "interleaved complex, contiguous batches",
                        "l2": f"{x.numel() * x.element_size() >> 20} MB input per exec > 129 MB L2; no flush"
                              if x.numel() * x.element_size() > (129 << 20) else "input fits L2",
-                       "parallelism": f"replicas x{world}"},
+                       "parallelism": f"batch shards x{world}", "global_batch": batch * world,
+                       "shard": [first, batch]},
             "gflops": round(gflops, 1),
             "hbm_frac": round(gbs / world / peak, 4),
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
