@@ -882,7 +882,9 @@ def run_ours(args):
 def run_peaks():
     """FMA throughput of the device (gfft_diag_fma_rate): the FP64 rate is
     the fp64 kernels' compute roof; fp32 against packed fp32x2 shows whether
-    the packed form raises the FP32 rate or only saves issue slots."""
+    the packed form raises the FP32 rate or only saves issue slots.  Read and
+    copy bandwidth (gfft_diag_mem_rate) over buffers below and above the L2
+    capacity: the ceiling of a pass whose intermediate stays in L2."""
     import torch
 
     import genfft_gb300 as G
@@ -894,6 +896,14 @@ def run_peaks():
         with ClockSampler(0) as clk:
             G._check(L.gfft_diag_fma_rate(which, ctypes.byref(tf), ctypes.byref(ms)))
         out[name] = {"tflops": round(tf.value, 3), "ms": round(ms.value, 4), "clocks": clk.summary()}
+    # read and copy bandwidth below and above the L2 capacity
+    mem = {}
+    for mb in (32, 64, 96, 128, 2048):
+        for mode, name in ((0, "read"), (1, "copy")):
+            gbs, ms = ctypes.c_double(), ctypes.c_double()
+            G._check(L.gfft_diag_mem_rate(mb << 20, mode, ctypes.byref(gbs), ctypes.byref(ms)))
+            mem[f"{name}_{mb}MB_gbs"] = round(gbs.value, 1)
+    out["memory"] = {"probe": "16-byte grid-stride loads / copies, 8 CTAs an SM, best of 5", **mem}
     print(json.dumps(out), flush=True)
     return 0
 

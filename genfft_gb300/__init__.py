@@ -75,6 +75,7 @@ SIGNATURES = {
     "gfft_fft_transform_noalloc": [_I, _I, _LL, _I, _P, _P, _P],
     "gfft_device_error": [ctypes.POINTER(_I)],
     "gfft_diag_fma_rate": [_I, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)],
+    "gfft_diag_mem_rate": [ctypes.c_longlong, _I, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)],
     "gfft_ragged_create": [ctypes.POINTER(_P), _I, ctypes.POINTER(_LL), _LL],
     "gfft_ragged_destroy": [_P],
     "gfft_ragged_exec": [_P, _I, _P, _P, _P],

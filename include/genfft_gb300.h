@@ -252,6 +252,11 @@ gfft_status gfft_device_error(int *code);
  * the best of five timed launches.  Allocates a 4-byte device buffer; it is
  * the denominator of the fp64 kernels' roofline. */
 gfft_status gfft_diag_fma_rate(int which, double *tflops, double *ms);
+/* Read (mode 0) or copy (mode 1) bandwidth over a device buffer of `bytes`
+ * bytes (1 MiB .. 8 GiB): below the L2 capacity the L2's rate, above it
+ * HBM's.  *gbs counts bytes read plus bytes written.  A probe, not a
+ * transform. */
+gfft_status gfft_diag_mem_rate(long long bytes, int mode, double *gbs, double *ms);
 
 const char *gfft_status_string(gfft_status status);
 /* message of the last failed call on this thread ("" if none) */
