@@ -9,7 +9,6 @@
 // (fp64) passes exchange through padded shared memory, and the last pass
 // stores straight to global memory.  Roofline: HBM-bound, 2 * N * 2 *
 // sizeof(T) algorithmic bytes per transform.
-#include <cstdlib>
 #include <mutex>
 
 #include "internal.h"
@@ -62,14 +61,9 @@ __global__ void __launch_bounds__(FusedCfg<T, LOGN>::THREADS, FusedCfg<T, LOGN>:
     const long long b = (long long)blockIdx.x * Cfg::TPC + g;
     const bool active = b < batch;
 
-    // Programmatic dependent launch (a no-op in an ordinary launch).  Once
-    // every CTA of this grid has started, the next kernel on the stream may
-    // be scheduled into the SM slots this grid's last wave frees; it still
-    // waits for this grid's completion before it reads (griddepcontrol.wait
-    // below, in the next launch).  This grid in turn waits for the previous
-    // kernel on the stream, and its writes, before the first read.
-    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-    asm volatile("griddepcontrol.wait;" ::: "memory");
+    // programmatic dependent launch: the next kernel's CTAs may fill the
+    // slots this grid's last wave frees; this grid waits for the previous one
+    pdl_enter();
     cpx<T> v[E];
     if (active) {
         const cpx<T> *src = in + b * idist + (long long)t * istride;
@@ -174,26 +168,7 @@ cudaError_t launch_fused_c2c(int dtype, int logn, int inverse, const FusedC2CArg
     void *args[] = {(void *)&in,      (void *)&out,     (void *)&batch, (void *)&idist, (void *)&odist,
                     (void *)&istride, (void *)&ostride, (void *)&tw,
                     dtype == GFFT_F32 ? (void *)&scale_f : (void *)&scale_d};
-    // launched as a programmatic dependent of the previous kernel on the
-    // stream (GFFT_PDL=0: an ordinary launch): the kernel waits for that
-    // kernel's completion before it reads, and its CTAs start while that
-    // kernel's last wave drains
-    static const bool pdl = [] {
-        const char *v = std::getenv("GFFT_PDL");
-        return !(v && *v == '0');
-    }();
-    if (!pdl) return cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(e.threads), args, e.smem, st);
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)grid);
-    cfg.blockDim = dim3(e.threads);
-    cfg.dynamicSmemBytes = e.smem;
-    cfg.stream = st;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    return cudaLaunchKernelExC(&cfg, fn, args);
+    return launch_pdl(fn, dim3((unsigned)grid), dim3(e.threads), args, e.smem, st);
 }
 
 }  // namespace gfft

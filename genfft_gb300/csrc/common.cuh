@@ -112,6 +112,17 @@ __device__ __forceinline__ cpx<T> ld_c(const cpx<T> *p)
     return {v.x, v.y};
 }
 // streaming (evict-first) global load / store for data touched once
+// Entry of a kernel launched as a programmatic dependent of the previous
+// kernel on the stream (launch_pdl; a no-op in an ordinary launch): let the
+// next kernel's CTAs be scheduled once every CTA of this grid has started,
+// then wait for the previous kernel's completion, and its writes, before
+// touching global memory.
+__device__ __forceinline__ void pdl_enter()
+{
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
 template <typename T>
 __device__ __forceinline__ cpx<T> ldcs_c(const cpx<T> *p)
 {

@@ -39,6 +39,12 @@ void fused_twiddle_fill(int dtype, int logn, void *host_buf);  // writes that ma
 cudaError_t launch_fused_c2c(int dtype, int logn, int inverse, const FusedC2CArgs &a,
                              cudaStream_t st);
 
+// Launches fn as a programmatic dependent of the previous kernel on the
+// stream: its CTAs may start while that kernel's last wave drains, and the
+// kernel (which begins with pdl_enter()) waits for that kernel's completion
+// before it touches global memory.  GFFT_PDL=0: an ordinary launch.
+cudaError_t launch_pdl(const void *fn, dim3 grid, dim3 block, void **args, size_t smem, cudaStream_t st);
+
 // ---- device twiddle cache (api.cpp) --------------------------------------
 // Returns a device pointer to the table made by `fill` (count complex
 // elements of dtype), cached per (device, key) for the process lifetime.

@@ -70,6 +70,7 @@ __global__ void __launch_bounds__(ColCfg<T, LOGL, C, E_>::THREADS)
     const long long col = (long long)blockIdx.x * C + s;
     const bool active = col < ncols;
     const unsigned lo_mask = (1u << lo_bits) - 1u;
+    pdl_enter();  // launched by launch_pdl: waits for the previous kernel
 
     {
         const long long b = blockIdx.y;
@@ -157,6 +158,7 @@ __global__ void __launch_bounds__(RowCfg<T, LOGL, C, E_>::THREADS)
     const long long row0 = (long long)blockIdx.x * C;
     const long long row = row0 + s;
     const bool active = row < nrows;
+    pdl_enter();  // launched by launch_pdl: waits for the previous kernel
 
     {
         const long long b = blockIdx.y;

@@ -55,6 +55,30 @@ int sm_count()
     return n;
 }
 
+}  // namespace
+
+cudaError_t launch_pdl(const void *fn, dim3 grid, dim3 block, void **args, size_t smem, cudaStream_t st)
+{
+    static const bool pdl = [] {
+        const char *v = std::getenv("GFFT_PDL");
+        return !(v && *v == '0');
+    }();
+    if (!pdl) return cudaLaunchKernel(fn, grid, block, args, smem, st);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelExC(&cfg, fn, args);
+}
+
+namespace {
+
 bool tma_disabled()
 {
     static const bool off = [] {
@@ -223,7 +247,7 @@ cudaError_t launch_colpass(const TileKernel &k, int inverse, long long tiles, lo
             void *args[] = {(void *)&map, (void *)&out, (void *)&ncols, (void *)&ld_out, (void *)&odist,
                             (void *)&nbatch, (void *)&tw, (void *)&tw_lo, (void *)&tw_hi, (void *)&lo_bits,
                             (void *)&nmask, (void *)&err, scale_p};
-            return cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(k.tma_threads), args, k.tma_smem, st);
+            return launch_pdl(fn, dim3((unsigned)grid), dim3(k.tma_threads), args, k.tma_smem, st);
         }
     }
     const void *fn = inverse ? k.inv : k.fwd;
@@ -238,7 +262,7 @@ cudaError_t launch_colpass(const TileKernel &k, int inverse, long long tiles, lo
         void *outp = static_cast<char *>(out) + b0 * odist * (long long)k.elem_bytes;
         args[0] = (void *)&inp;
         args[1] = (void *)&outp;
-        e = cudaLaunchKernel(fn, dim3((unsigned)tiles, (unsigned)nb), dim3(k.threads), args, k.smem, st);
+        e = launch_pdl(fn, dim3((unsigned)tiles, (unsigned)nb), dim3(k.threads), args, k.smem, st);
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
@@ -260,7 +284,7 @@ cudaError_t launch_rowpass(const TileKernel &k, int inverse, long long tiles, lo
         const long long grid = persistent_grid(fn, k.tma_threads, k.tma_smem, tiles * nbatch);
         void *args[] = {(void *)&in,    (void *)&out,   (void *)&nrows, (void *)&ld_in, (void *)&ostride,
                         (void *)&idist, (void *)&odist, (void *)&nbatch, (void *)&tw, (void *)&err, scale_p};
-        return cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(k.tma_threads), args, k.tma_smem, st);
+        return launch_pdl(fn, dim3((unsigned)grid), dim3(k.tma_threads), args, k.tma_smem, st);
     }
     const void *fn = inverse ? k.inv : k.fwd;
     cudaError_t e = ensure_smem(fn, k.smem);
@@ -271,7 +295,7 @@ cudaError_t launch_rowpass(const TileKernel &k, int inverse, long long tiles, lo
         void *outp = static_cast<char *>(out) + b0 * odist * (long long)k.elem_bytes;
         void *args[] = {(void *)&inp,   (void *)&outp,  (void *)&nrows, (void *)&ld_in,
                         (void *)&ostride, (void *)&idist, (void *)&odist, (void *)&tw, scale_p};
-        e = cudaLaunchKernel(fn, dim3((unsigned)tiles, (unsigned)nb), dim3(k.threads), args, k.smem, st);
+        e = launch_pdl(fn, dim3((unsigned)tiles, (unsigned)nb), dim3(k.threads), args, k.smem, st);
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;

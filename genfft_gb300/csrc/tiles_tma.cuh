@@ -67,6 +67,7 @@ __global__ void __launch_bounds__(RowTmaCfg<T, LOGL, C, E_, NSTG>::THREADS, 1)
     const int t = threadIdx.x - s * G;
     const long long tiles = (nrows + C - 1) / C;
     const long long total = tiles * nbatch;
+    pdl_enter();  // launched by launch_pdl: waits for the previous kernel
 
     if (threadIdx.x == 0) {
         for (int i = 0; i < NSTG; i++) mbar_init(&bars[i], 1);
@@ -189,6 +190,7 @@ __global__ void __launch_bounds__(ColTmaCfg<T, LOGL, C, E_, NSTG>::THREADS, 1)
     const long long tiles = (ncols + C - 1) / C;
     const long long total = tiles * nbatch;
     const unsigned lo_mask = (1u << lo_bits) - 1u;
+    pdl_enter();  // launched by launch_pdl: waits for the previous kernel
 
     if (threadIdx.x == 0) {
         for (int i = 0; i < NSTG; i++) mbar_init(&bars[i], 1);
