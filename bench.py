@@ -424,14 +424,19 @@ def run_reference(args):
 def kernel_name(G, kind, dtype, n0, mode=0, launches=1):
     """The kernels of one exec of the workload (`launches`: the plan's
     launch count for the batch; the four-step path is one persistent
-    launch, or column + row tile launches per workspace group)."""
+    launch, column + row tile launches per workspace group, or, for fp32
+    2^21 .. 2^24, three short-tile passes per group)."""
     if mode:
         return "k_tc"
     fused = n0 <= G.max_fused_size(G.F32 if dtype == "f32" else G.F64)
     if kind == "c2c":
         if fused:
             return "k_c2c_fused"
-        return "k_fourstep" if launches == 1 else "k_colpass_tma + k_rowpass_tma"
+        if launches == 1:
+            return "k_fourstep"
+        if launches % 3 == 0 and dtype == "f32" and n0 >= (1 << 21):
+            return "k3_col (two column passes) + k3_row"
+        return "k_colpass_tma + k_rowpass_tma"
     if kind == "c2r":
         return "k_c2r_fused" if n0 // 2 <= G.max_fused_size(G.F32) else "C2R pre-pass + four-step inverse"
     if kind == "r2c":

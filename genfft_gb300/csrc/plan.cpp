@@ -6,6 +6,8 @@
 //   C2C  n <= 2^14 (fp32) / 2^13 (fp64)  one fused kernel (c2c_fused.cu)
 //        fp32 2^16 .. 2^19               the persistent four-step kernel
 //                                        (fourstep.cuh), one launch a batch
+//        fp32 2^21 .. 2^24               three passes of short tiles
+//                                        (threepass.cu) per workspace group
 //        otherwise                       column + row tile launches per
 //                                        workspace group (tiles*.cuh), the
 //                                        widest TMA-pipelined tile that fits
@@ -101,6 +103,35 @@ void C2CCore::init(int dtype_, int logn_, long long batch_hint, int path, bool r
     krow = tile_find(dtype, TILE_ROW_XPOSE, logB, crow);
     tw_col = tile_table(dtype, kcol, logA, ccol);
     tw_row = tile_table(dtype, krow, logB, crow);
+
+    // three passes of short tiles (threepass.cu), through a workspace of the
+    // tile launches' size (GFFT_3PASS=1 / 0 overrides the measured default)
+    const ThreePass *tpk = threepass_find(dtype, logn);
+    // measured on GB300 (1 GB batches, forward + inverse, GB/s, two passes
+    // against three): 2^19 2028 / 1892, 2^20 2136 / 2067, 2^21 2006 / 2117,
+    // 2^22 1870 / 2041, 2^23 1789 / 1978, 2^24 1554 / 1934
+    const bool tp_default = logn >= 21;
+    // (an explicit request for the persistent kernels, GFFT_FS=1 or
+    // GFFT_FS_PAIR=1, keeps them)
+    const long long want_tp = env_ll("GFFT_3PASS", -1);
+    const bool fs_asked = env_ll("GFFT_FS", 0) != 0 || env_ll("GFFT_FS_PAIR", 0) != 0;
+    if (tpk && path < 0 && !real_rows && (want_tp > 0 || (want_tp < 0 && tp_default && !fs_asked))) {
+        tp = tpk;
+        for (int p = 0; p < 3; p++) {
+            const int l = p == 0 ? tp->la : p == 1 ? tp->lb : tp->lc;
+            const ThreePass *k = tp;
+            tp_tw[p] = cached_table("tp/" + std::to_string(d) + "/" + std::to_string(l), d, k->tw_count[p],
+                                    [k, p](void *buf) { k->tw_fill[p](buf); });
+        }
+        wn_tables(dtype, tp->lb + tp->lc, &tp_bits2, &tp_lo2, &tp_hi2);
+        const long long budget = env_ll("GFFT_WS_BUDGET_MB", 1024) << 20;
+        group = std::max<long long>(1, budget / (N * (long long)cplx_bytes(dtype)));
+        group = std::min(group, std::max<long long>(1, batch_hint));
+        ws_bytes = (size_t)(group * N) * cplx_bytes(dtype);
+        check_cuda(cudaMalloc(&ws, ws_bytes), "cudaMalloc(workspace)");
+        algo = 5;
+        return;
+    }
 
     int nall = 0;
     const FourStepKernel *const *all = fourstep_variants(dtype, logn, &nall);
@@ -210,6 +241,7 @@ static long long fs_chunk(int items_per_transform, int lag)
 int C2CCore::launches(long long batch) const
 {
     if (algo == 1) return 1;
+    if (algo == 5) return 3 * (int)((batch + group - 1) / group);
     if (algo == 3) {
         const long long chunk = fs_chunk(fs->nc + fs_nr, fs_lag);
         return (int)((batch + chunk - 1) / chunk);
@@ -227,6 +259,18 @@ void C2CCore::run(int inverse, const void *in, void *out, long long batch, long 
     }
     if (istride != 1 || ostride != 1)
         fail(GFFT_ERR_UNSUPPORTED, "lengths above the fused limit need unit element strides");
+    if (algo == 5) {
+        const size_t eb5 = cplx_bytes(dtype);
+        for (long long g0 = 0; g0 < batch; g0 += group) {
+            const long long nb = std::min(group, batch - g0);
+            ThreePassArgs a{static_cast<const char *>(in) + (size_t)(g0 * idist) * eb5,
+                            static_cast<char *>(out) + (size_t)(g0 * odist) * eb5,
+                            ws, nb, idist, odist, {tp_tw[0], tp_tw[1], tp_tw[2]}, tw_lo, tw_hi, lo_bits,
+                            tp_lo2, tp_hi2, tp_bits2, scale};
+            check_cuda(launch_threepass(*tp, inverse, a, st), "launch three-pass C2C");
+        }
+        return;
+    }
     if (algo == 3 && !fs_real && run_persistent(inverse, in, out, batch, idist, odist, st, scale)) return;
     const long long A = 1LL << logA, B = 1LL << logB, N = A * B;
     const size_t eb = cplx_bytes(dtype);

@@ -8,6 +8,7 @@
 
 #include "internal.h"
 #include "fourstep.h"
+#include "threepass.h"
 #include "tiles_registry.h"
 
 namespace gfft {
@@ -20,10 +21,15 @@ bool is_pow2(long long n);
 // memory limit, else the four-step column + row passes through a workspace.
 struct C2CCore {
     int dtype = 0, logn = 0;
-    int algo = 0;  // 1 fused, 2 four-step tile launches, 3 persistent four-step
+    int algo = 0;  // 1 fused, 2 four-step tile launches, 3 persistent four-step, 5 three passes
     const void *tw = nullptr;
     // persistent four-step: kernel, ring of `fs_slots` transforms, counters
     const FourStepKernel *fs = nullptr;
+    // algo 5: three passes of short tiles (threepass.cu) through `ws`
+    const ThreePass *tp = nullptr;
+    const void *tp_tw[3] = {};
+    const void *tp_lo2 = nullptr, *tp_hi2 = nullptr;  // W_(n / 2^la) tables of pass 2
+    int tp_bits2 = 0;
     int fs_slots = 0, fs_lag = 0, fs_grid = 0;
     int fs_nr = 0;            // row items per transform
     bool fs_real = false;     // real-input mode: the kernel's DIT version
