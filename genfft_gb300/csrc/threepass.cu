@@ -17,9 +17,11 @@
 // through the workspace.  Replaces FFT<float>::transform<inv> (fft.h:80-85)
 // for these lengths.
 #include <algorithm>
+#include <cstdlib>
 #include <map>
 #include <mutex>
 #include <utility>
+#include <vector>
 
 #include "internal.h"
 #include "threepass.h"
@@ -138,9 +140,9 @@ struct Minb {
     static constexpr int value = 1024 / THREADS > 8 ? 8 : 1024 / THREADS;
 };
 
-std::map<int, ThreePass> &tp_registry()
+std::map<int, std::vector<ThreePass>> &tp_registry()
 {
-    static std::map<int, ThreePass> r;
+    static std::map<int, std::vector<ThreePass>> r;
     return r;
 }
 std::mutex &tp_mu()
@@ -181,17 +183,26 @@ struct TpReg {
         k.tw_fill[1] = &tp_fill<B>;
         k.tw_fill[2] = &tp_fill<CC>;
         std::lock_guard<std::mutex> lk(tp_mu());
-        tp_registry()[A + B + CC] = k;
+        tp_registry()[A + B + CC].push_back(k);
     }
 };
 
 // (a, b, c, pass-1 columns, pass-2 columns, pass-3 rows): tiles of 2048 -
-// 4096 points, runs of 16 - 64 points
+// 4096 points, runs of 16 - 64 points.  The first layout of a length is
+// the default, the others are selected by GFFT_3PASS_VARIANT.  Measured on
+// GB300 (GB/s, 1 GB batches, forward + inverse):
+//   2^21  (7,7,7 | 32,32,16) 2118   (7,6,8 | 32,64,16) 2057
+//   2^22  (7,7,8 | 32,32,16) 2095   (7,8,7 | 32,16,16) 2040, four other
+//         shapes 1951-2044
+//   2^23  (7,8,8 | 32,16,16) 2017   (8,7,8 | 16,32,16) 1978
 TpReg<6, 7, 6, 64, 32, 32> tp19;
 TpReg<7, 6, 7, 32, 64, 16> tp20;
 TpReg<7, 7, 7, 32, 32, 16> tp21;
-TpReg<7, 8, 7, 32, 16, 16> tp22;
-TpReg<8, 7, 8, 16, 32, 16> tp23;
+TpReg<7, 6, 8, 32, 64, 16> tp21_1;
+TpReg<7, 7, 8, 32, 32, 16> tp22;
+TpReg<7, 8, 7, 32, 16, 16> tp22_1;
+TpReg<7, 8, 8, 32, 16, 16> tp23;
+TpReg<8, 7, 8, 16, 32, 16> tp23_1;
 TpReg<8, 8, 8, 16, 16, 16> tp24;
 
 cudaError_t opt_in(const void *fn, size_t smem)
@@ -213,9 +224,14 @@ cudaError_t opt_in(const void *fn, size_t smem)
 const ThreePass *threepass_find(int dtype, int logn)
 {
     if (dtype != GFFT_F32) return nullptr;
+    static const int variant = [] {
+        const char *v = std::getenv("GFFT_3PASS_VARIANT");
+        return (v && *v) ? std::atoi(v) : 0;
+    }();
     std::lock_guard<std::mutex> lk(tp_mu());
     auto it = tp_registry().find(logn);
-    return it == tp_registry().end() ? nullptr : &it->second;
+    if (it == tp_registry().end() || it->second.empty()) return nullptr;
+    return &it->second[variant >= 0 && variant < (int)it->second.size() ? variant : 0];
 }
 
 cudaError_t launch_threepass(const ThreePass &k, int inverse, const ThreePassArgs &a, cudaStream_t st)
