@@ -17,10 +17,11 @@
 
 namespace gfft {
 
-// points per thread: radix-16 registers for fp32, radix-8 for fp64
-template <typename T>
+// points per thread: radix-16 registers for fp32, radix-8 for fp64;
+// radix-32 for fp32 2^13 and 2^14 (three passes instead of four)
+template <typename T, int LOGN>
 struct FusedE {
-    static constexpr int value = sizeof(T) == 4 ? 16 : 8;
+    static constexpr int value = sizeof(T) == 4 ? ((LOGN == 13 || LOGN == 14) ? 32 : 16) : 8;
 };
 
 template <typename T>
@@ -32,7 +33,7 @@ struct FusedMax {
 // threads, else several transforms share the CTA
 template <typename T, int LOGN>
 struct FusedCfg {
-    using SP = StockhamPlan<T, LOGN, FusedE<T>::value>;
+    using SP = StockhamPlan<T, LOGN, FusedE<T, LOGN>::value>;
     static constexpr int TPC = SP::G >= 256 ? 1 : 256 / SP::G;
     static constexpr int THREADS = SP::G * TPC;
     static constexpr size_t SMEM = (size_t)SP::SMEM * TPC * sizeof(cpx<T>);
@@ -41,6 +42,8 @@ struct FusedCfg {
     // 256 threads (the residency the compiler picked unconstrained) and two
     // for 512-thread CTAs
     static constexpr int MIN_BLOCKS = (sizeof(T) == 4 && (LOGN == 12 || (LOGN >= 5 && LOGN <= 8))) ? 4
+                                    : (sizeof(T) == 4 && LOGN == 13) ? 2
+                                    : (sizeof(T) == 4 && LOGN == 14) ? 1
                                     : THREADS <= 256 ? 3 : THREADS <= 512 ? 2 : 1;
 };
 
@@ -74,7 +77,7 @@ __global__ void __launch_bounds__(FusedCfg<T, LOGN>::THREADS, FusedCfg<T, LOGN>:
         for (int q = 0; q < E; q++) v[q] = cpx<T>{(T)0, (T)0};
     }
     cpx<T> *my = sm + g * SP::SMEM;
-    stockham_run<T, LOGN, FusedE<T>::value, INV>(
+    stockham_run<T, LOGN, FusedE<T, LOGN>::value, INV>(
         v, t, [my](int i) -> cpx<T> & { return my[spad<T>(i)]; }, tw, []() { __syncthreads(); });
     if (active) {
         cpx<T> *dst = out + b * odist + (long long)t * ostride;
@@ -91,7 +94,7 @@ namespace {
 template <typename T, int LOGN>
 void fill_tw(void *buf)
 {
-    stockham_fill_twiddles<T, LOGN, FusedE<T>::value>(
+    stockham_fill_twiddles<T, LOGN, FusedE<T, LOGN>::value>(
         static_cast<cpx<T> *>(buf), [](long long k, long long M, cpx<T> *w) { forward_root<T>(k, M, &w->x, &w->y); });
 }
 
