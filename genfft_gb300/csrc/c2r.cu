@@ -65,27 +65,32 @@ __device__ __forceinline__ cpx<T> c2r_pre_value(cpx<T> fk, cpx<T> fp, cpx<T> t)
     return {s.x + m.x, s.y + m.y};
 }
 
-template <typename T, int LOGH>
+template <typename T, int LOGH, int W>
 struct C2RCfg {
     using SP = StockhamPlan<T, LOGH, C2RE<T>::value>;
     static constexpr int H = SP::N;
     static constexpr int TPC = SP::G >= 256 ? 1 : 256 / SP::G;
     static constexpr int THREADS = SP::G * TPC;
     static constexpr int SPAD = spad_size<T>(H);
-    static constexpr int SMEM_T = SPAD > 2 * H + 1 ? SPAD : 2 * H + 1;
+    // shared slots a transform: its input bins (H + 1, or 2H for the folded
+    // full spectrum), then the Stockham exchanges
+    static constexpr int NIN = W == W_FOLD_FULL ? 2 * H : H + 1;
+    static constexpr int SMEM_T = SPAD > NIN ? SPAD : NIN;
     static constexpr size_t SMEM = (size_t)SMEM_T * TPC * sizeof(cpx<T>);
 };
+// the most dynamic shared memory a CTA can opt in to on GB300 (227 KB)
+constexpr size_t C2R_SMEM_MAX = 227 * 1024;
 
 // in: bins (idist complex between transforms), out: reals (odist reals, even)
 template <typename T, int LOGH, int W>
-__global__ void __launch_bounds__(C2RCfg<T, LOGH>::THREADS)
+__global__ void __launch_bounds__(C2RCfg<T, LOGH, W>::THREADS)
     k_c2r_fused(const cpx<T> *__restrict__ in, T *__restrict__ out, long long batch, long long idist,
                 long long odist, const cpx<T> *__restrict__ tw, const cpx<T> *__restrict__ dtw, T scale)
 {
-    using Cfg = C2RCfg<T, LOGH>;
+    using Cfg = C2RCfg<T, LOGH, W>;
     using SP = typename Cfg::SP;
     constexpr int E = SP::E, G = SP::G, H = SP::N;
-    constexpr int NIN = W == W_FOLD_FULL ? 2 * H : H + 1;
+    constexpr int NIN = Cfg::NIN;
     extern __shared__ unsigned char smem_raw[];
     cpx<T> *sm = reinterpret_cast<cpx<T> *>(smem_raw);
     const int g = threadIdx.x / G;
@@ -169,16 +174,18 @@ cudaError_t smem_optin2(const void *fn, size_t smem)
 struct C2REntry {
     const void *fn[3];
     int threads, tpc;
-    size_t smem;
+    size_t smem[3];  // per weight mode
 };
 
 template <typename T, int LOGH>
 C2REntry make_c2r()
 {
-    using Cfg = C2RCfg<T, LOGH>;
+    using Cfg = C2RCfg<T, LOGH, W_PLAIN>;
     return C2REntry{{(const void *)&k_c2r_fused<T, LOGH, W_PLAIN>, (const void *)&k_c2r_fused<T, LOGH, W_HALF_INTERIOR>,
                      (const void *)&k_c2r_fused<T, LOGH, W_FOLD_FULL>},
-                    Cfg::THREADS, Cfg::TPC, Cfg::SMEM};
+                    Cfg::THREADS,
+                    Cfg::TPC,
+                    {Cfg::SMEM, C2RCfg<T, LOGH, W_HALF_INTERIOR>::SMEM, C2RCfg<T, LOGH, W_FOLD_FULL>::SMEM}};
 }
 
 template <typename T, int... L>
@@ -219,19 +226,26 @@ void pre_launch(int w, unsigned g, const void *in, void *out, long long H, long 
 
 int c2r_fused_max_logh(int dtype) { return dtype == GFFT_F32 ? C2RMax<float>::value : C2RMax<double>::value; }
 
+bool c2r_fused_fits(int dtype, int logh, int wmode)
+{
+    return logh <= c2r_fused_max_logh(dtype) && c2r_entry(dtype, logh).smem[wmode] <= C2R_SMEM_MAX;
+}
+
 cudaError_t launch_c2r_fused(int dtype, int logh, int wmode, const void *in, void *out, long long batch,
                              long long idist, long long odist, const void *tw, const void *dtw, cudaStream_t st,
                              double scale)
 {
     const C2REntry &e = c2r_entry(dtype, logh);
     const void *fn = e.fn[wmode];
-    cudaError_t err = smem_optin2(fn, e.smem);
+    const size_t smem = e.smem[wmode];
+    if (smem > C2R_SMEM_MAX) return cudaErrorInvalidValue;  // the planner routes these elsewhere
+    cudaError_t err = smem_optin2(fn, smem);
     if (err != cudaSuccess) return err;
     const long long grid = (batch + e.tpc - 1) / e.tpc;
     float scale_f = (float)scale;
     void *args[] = {(void *)&in,  (void *)&out, (void *)&batch, (void *)&idist, (void *)&odist, (void *)&tw,
                     (void *)&dtw, dtype == GFFT_F32 ? (void *)&scale_f : (void *)&scale};
-    return cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(e.threads), args, e.smem, st);
+    return cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(e.threads), args, smem, st);
 }
 
 cudaError_t launch_c2r_pre(int dtype, int wmode, const void *in, void *out, long long H, long long batch,

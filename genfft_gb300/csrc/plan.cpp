@@ -585,12 +585,16 @@ void C2RCore::init(int dtype_, int logn_, long long batch_hint)
     const int d = dtype, l = logn, lh = logn - 1;
     dtw = cached_table("dit/" + std::to_string(d) + "/" + std::to_string(l), d, (1LL << lh) + 1,
                        [d, l](void *buf) { dit_twiddle_fill(d, l, buf); });
-    if (lh <= c2r_fused_max_logh(dtype)) {
+    if (c2r_fused_fits(dtype, lh, 0)) {
         // the fused C2R runs the same Stockham plan (points per thread) as
         // the fused R2C of this half length, so it shares that table
         algo = 1;
         tw = cached_table("r2c/" + std::to_string(d) + "/" + std::to_string(lh), d, r2c_twiddle_count(d, lh),
                           [d, lh](void *buf) { r2c_twiddle_fill(d, lh, buf); });
+        if (!c2r_fused_fits(dtype, lh, 2)) {
+            fold_split = true;
+            c2c.init(dtype, lh, batch_hint);
+        }
         return;
     }
     algo = 2;
@@ -608,7 +612,7 @@ void C2RCore::run(const void *in, void *out, long long batch, long long idist, l
 {
     if (algo == 0) {
         check_cuda(launch_c2r_one(dtype, in, out, batch, idist, odist, st, scale), "launch C2R n=1");
-    } else if (algo == 1) {
+    } else if (algo == 1 && !(fold_split && wmode == 2)) {
         check_cuda(launch_c2r_fused(dtype, logn - 1, wmode, in, out, batch, idist, odist, tw, dtw, st, scale),
                    "launch fused C2R");
     } else {

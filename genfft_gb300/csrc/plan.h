@@ -135,6 +135,9 @@ struct C2RCore {
     int dtype = 0, logn = 0;
     int algo = 0;  // 0 n == 1, 1 fused, 2 pre-pass + C2C(n/2) inverse
     const void *tw = nullptr, *dtw = nullptr;
+    // algo 1 whose folded full-spectrum input (2 n/2 bins) does not fit the
+    // fused kernel's shared memory: that mode takes the algo 2 route
+    bool fold_split = false;
     C2CCore c2c;
     void init(int dtype, int logn, long long batch_hint);
     void release() { c2c.release(); }
@@ -176,6 +179,10 @@ cudaError_t launch_dit(int dtype, int mode, const void *in, void *out, long long
 // bins halved (adjoint of the half-spectrum R2C), 2 = n-bin input folded
 // (g_k + conj g_{n-k}) / 2 (adjoint of the full-spectrum R2C)
 int c2r_fused_max_logh(int dtype);
+// whether the fused C2R holds a transform of half length 2^logh with the
+// input weighting wmode (0 plain, 1 halved interior, 2 folded full spectrum)
+// in one CTA's shared memory
+bool c2r_fused_fits(int dtype, int logh, int wmode);
 cudaError_t launch_c2r_fused(int dtype, int logh, int wmode, const void *in, void *out, long long batch,
                              long long idist, long long odist, const void *tw, const void *dtw, cudaStream_t st,
                              double scale = 1.0);

@@ -70,7 +70,7 @@ def test_c2c_gradient(gfft, n, inverse):
 
 
 @pytest.mark.parametrize("n,half", [(2, True), (8, True), (64, False), (4096, True), (4096, False),
-                                    (1 << 16, True), (1 << 20, True)])
+                                    (1 << 15, True), (1 << 15, False), (1 << 16, True), (1 << 20, True)])
 def test_r2c_gradient_hermitian_weighting(gfft, n, half):
     import torch
     from genfft_gb300 import autograd as A
@@ -97,7 +97,7 @@ def test_r2c_gradient_hermitian_weighting(gfft, n, half):
     assert err < 1, err
 
 
-@pytest.mark.parametrize("n", [2, 16, 4096, 1 << 17])
+@pytest.mark.parametrize("n", [2, 16, 4096, 1 << 14, 1 << 15, 1 << 17])
 def test_c2r_forward_and_gradient(gfft, n):
     import torch
     from genfft_gb300 import autograd as A
@@ -152,3 +152,38 @@ def test_gradcheck_fp64(gfft):
     yr[:, -1] = yr[:, -1].real
     yr.requires_grad_(True)
     assert torch.autograd.gradcheck(lambda v: A.irfft(v, 32), (yr,))
+
+
+@pytest.mark.parametrize("dt,logn", [("f32", 14), ("f32", 15), ("f64", 13), ("f64", 14)])
+def test_c2r_at_the_fused_limit(gfft, dt, logn):
+    """Half lengths at the fused C2R's shared-memory limit (fp32 2^14, fp64
+    2^13): the plain half-spectrum inverse runs fused, and the adjoint of
+    the full-spectrum R2C (2 n/2 folded bins, too many for one CTA there)
+    takes the pre-pass + C2C route; both against FP64."""
+    import torch
+    n, batch = 1 << logn, 3
+    f32 = dt == "f32"
+    rdt, cdt = (torch.float32, torch.complex64) if f32 else (torch.float64, torch.complex128)
+    code = gfft.F32 if f32 else gfft.F64
+    tol = (2e-7 if f32 else 1e-15) * logn
+    rng = np.random.default_rng(logn + (0 if f32 else 50))
+    m = n // 2 + 1
+    yn = rng.standard_normal((batch, m)) + 1j * rng.standard_normal((batch, m))
+    yn[:, 0] = yn[:, 0].real
+    yn[:, -1] = yn[:, -1].real
+    half = gfft.Plan(gfft.KIND_R2C, code, n, 0, batch, gfft.FLAG_HALF_SPECTRUM)
+    y = torch.tensor(yn, dtype=cdt, device="cuda")
+    x = torch.empty(batch, n, dtype=rdt, device="cuda")
+    half.exec(x, y, True)
+    torch.cuda.synchronize()
+    ref = np.fft.irfft(yn, n) * n
+    assert np.linalg.norm(x.cpu().numpy() - ref) / np.linalg.norm(ref) <= tol
+    # adjoint of the full-spectrum R2C: x_j = Re sum_k g_k exp(+2 pi i jk/n)
+    gn = rng.standard_normal((batch, n)) + 1j * rng.standard_normal((batch, n))
+    full = gfft.Plan(gfft.KIND_R2C, code, n, 0, batch)
+    g = torch.tensor(gn, dtype=cdt, device="cuda")
+    xa = torch.empty(batch, n, dtype=rdt, device="cuda")
+    full.adjoint(xa, g)
+    torch.cuda.synchronize()
+    an = (np.fft.ifft(gn) * n).real
+    assert np.linalg.norm(xa.cpu().numpy() - an) / np.linalg.norm(an) <= tol
