@@ -29,9 +29,11 @@ namespace gfft {
 
 enum C2RWeight { W_PLAIN = 0, W_HALF_INTERIOR = 1, W_FOLD_FULL = 2 };
 
-template <typename T>
+// points per thread: the same as the R2C kernels (real.cu), whose twiddle
+// table this kernel shares
+template <typename T, int LOGH>
 struct C2RE {
-    static constexpr int value = sizeof(T) == 4 ? 16 : 8;
+    static constexpr int value = sizeof(T) == 4 ? ((LOGH == 13 || LOGH == 14) ? 32 : 16) : 8;
 };
 template <typename T>
 struct C2RMax {
@@ -67,7 +69,7 @@ __device__ __forceinline__ cpx<T> c2r_pre_value(cpx<T> fk, cpx<T> fp, cpx<T> t)
 
 template <typename T, int LOGH, int W>
 struct C2RCfg {
-    using SP = StockhamPlan<T, LOGH, C2RE<T>::value>;
+    using SP = StockhamPlan<T, LOGH, C2RE<T, LOGH>::value>;
     static constexpr int H = SP::N;
     static constexpr int TPC = SP::G >= 256 ? 1 : 256 / SP::G;
     static constexpr int THREADS = SP::G * TPC;
@@ -113,7 +115,7 @@ __global__ void __launch_bounds__(C2RCfg<T, LOGH, W>::THREADS)
         v[q] = c2r_pre_value(c2r_bin<W, T>(get, k, H), c2r_bin<W, T>(get, p, H), ldg_c(dtw + k));
     }
     __syncthreads();
-    stockham_run<T, LOGH, C2RE<T>::value, true>(
+    stockham_run<T, LOGH, C2RE<T, LOGH>::value, true>(
         v, t, [my](int i) -> cpx<T> & { return my[spad<T>(i)]; }, tw, []() { __syncthreads(); });
     if (active) {
         cpx<T> *dst = reinterpret_cast<cpx<T> *>(out + b * odist) + t;

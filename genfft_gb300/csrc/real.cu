@@ -25,9 +25,11 @@
 
 namespace gfft {
 
-template <typename T>
+// points per thread of the n/2-point C2C: 16 (fp32) / 8 (fp64); 32 for fp32
+// half lengths 2^13 and 2^14 (three radix-32 passes instead of four)
+template <typename T, int LOGH>
 struct RealE {
-    static constexpr int value = sizeof(T) == 4 ? 16 : 8;
+    static constexpr int value = sizeof(T) == 4 ? ((LOGH == 13 || LOGH == 14) ? 32 : 16) : 8;
 };
 template <typename T>
 struct RealMax {  // log2 of the largest fused half length
@@ -36,7 +38,7 @@ struct RealMax {  // log2 of the largest fused half length
 
 template <typename T, int LOGH>
 struct R2CCfg {
-    using SP = StockhamPlan<T, LOGH, RealE<T>::value>;
+    using SP = StockhamPlan<T, LOGH, RealE<T, LOGH>::value>;
     static constexpr int TPC = SP::G >= 256 ? 1 : 256 / SP::G;
     static constexpr int THREADS = SP::G * TPC;
     static constexpr int SMEM_T = spad_size<T>(SP::N);
@@ -83,7 +85,7 @@ __global__ void __launch_bounds__(R2CCfg<T, LOGH>::THREADS)
 #pragma unroll
         for (int q = 0; q < E; q++) v[q] = cpx<T>{(T)0, (T)0};
     }
-    stockham_run<T, LOGH, RealE<T>::value, false>(
+    stockham_run<T, LOGH, RealE<T, LOGH>::value, false>(
         v, t, [my](int i) -> cpx<T> & { return my[spad<T>(i)]; }, tw, []() { __syncthreads(); });
     __syncthreads();
 #pragma unroll
@@ -235,7 +237,7 @@ struct R2CEntry {
 template <typename T, int LOGH>
 void r2c_fill(void *buf)
 {
-    stockham_fill_twiddles<T, LOGH, RealE<T>::value>(
+    stockham_fill_twiddles<T, LOGH, RealE<T, LOGH>::value>(
         static_cast<cpx<T> *>(buf), [](long long k, long long M, cpx<T> *w) { forward_root<T>(k, M, &w->x, &w->y); });
 }
 
