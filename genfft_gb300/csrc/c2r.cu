@@ -102,8 +102,24 @@ __global__ void __launch_bounds__(C2RCfg<T, LOGH, W>::THREADS)
     cpx<T> *my = sm + g * Cfg::SMEM_T;
 
     if (active) {
+        // E loads in flight a thread (a loop of one load and one store a
+        // step keeps a single load in flight), then their stores
         const cpx<T> *src = in + b * idist;
-        for (int i = t; i < NIN; i += G) my[i] = ldcs_c(src + i);
+        constexpr int PER = (NIN + G - 1) / G;
+#pragma unroll
+        for (int c0 = 0; c0 < PER; c0 += E) {
+            cpx<T> tmp[E];
+#pragma unroll
+            for (int j = 0; j < E; j++) {
+                const int i = t + (c0 + j) * G;
+                if (c0 + j < PER && i < NIN) tmp[j] = ldcs_c(src + i);
+            }
+#pragma unroll
+            for (int j = 0; j < E; j++) {
+                const int i = t + (c0 + j) * G;
+                if (c0 + j < PER && i < NIN) my[i] = tmp[j];
+            }
+        }
     }
     __syncthreads();
     cpx<T> v[E];
