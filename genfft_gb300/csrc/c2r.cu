@@ -100,6 +100,7 @@ __global__ void __launch_bounds__(C2RCfg<T, LOGH, W>::THREADS)
     const long long b = (long long)blockIdx.x * Cfg::TPC + g;
     const bool active = b < batch;
     cpx<T> *my = sm + g * Cfg::SMEM_T;
+    pdl_enter();  // launched by launch_pdl: waits for the previous kernel
 
     if (active) {
         // E loads in flight a thread (a loop of one load and one store a
@@ -263,7 +264,7 @@ cudaError_t launch_c2r_fused(int dtype, int logh, int wmode, const void *in, voi
     float scale_f = (float)scale;
     void *args[] = {(void *)&in,  (void *)&out, (void *)&batch, (void *)&idist, (void *)&odist, (void *)&tw,
                     (void *)&dtw, dtype == GFFT_F32 ? (void *)&scale_f : (void *)&scale};
-    return cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(e.threads), args, smem, st);
+    return launch_pdl(fn, dim3((unsigned)grid), dim3(e.threads), args, smem, st);
 }
 
 cudaError_t launch_c2r_pre(int dtype, int wmode, const void *in, void *out, long long H, long long batch,

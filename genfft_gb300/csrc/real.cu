@@ -75,6 +75,7 @@ __global__ void __launch_bounds__(R2CCfg<T, LOGH>::THREADS)
     const long long b = (long long)blockIdx.x * Cfg::TPC + g;
     const bool active = b < batch;
     cpx<T> *my = sm + g * Cfg::SMEM_T;
+    pdl_enter();  // launched by launch_pdl: waits for the previous kernel
 
     cpx<T> v[E];
     if (active) {
@@ -307,7 +308,7 @@ cudaError_t launch_r2c_fused(int dtype, int logh, int mode, const void *in, void
     float scale_f = (float)scale;
     void *args[] = {(void *)&in,  (void *)&out, (void *)&batch, (void *)&idist, (void *)&odist, (void *)&tw,
                     (void *)&dtw, dtype == GFFT_F32 ? (void *)&scale_f : (void *)&scale};
-    return cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(e.threads), args, e.smem, st);
+    return launch_pdl(fn, dim3((unsigned)grid), dim3(e.threads), args, e.smem, st);
 }
 
 template <typename T>

@@ -60,6 +60,7 @@ __global__ void __launch_bounds__(RowDitCfg<T, LOGB, CH, E_>::THREADS, 1024 / Ro
     const bool row0 = p == P;  // the block of row 0 (self-paired)
     const long long b = blockIdx.y;
     const long long H = A * B;
+    pdl_enter();  // launched by launch_pdl: waits for the previous kernel
     const int s = threadIdx.x / G, t = threadIdx.x - s * G;
     // row of slot s: lo slots 1 + CH p + s, hi slots their mirrors A - k1
     long long k1;
@@ -177,7 +178,7 @@ cudaError_t launch_rowpass_dit(const RowDitKernel &k, const void *in, void *out,
         void *dst = static_cast<char *>(out) + (size_t)(b0 * odist) * 8;
         void *args[] = {(void *)&src, (void *)&dst, (void *)&A, (void *)&idist, (void *)&odist, (void *)&tw,
                         (void *)&dtw, (void *)&scale_f};
-        cudaError_t e = cudaLaunchKernel(k.fn, dim3((unsigned)blocks, (unsigned)nb), dim3(k.threads), args, k.smem, st);
+        cudaError_t e = launch_pdl(k.fn, dim3((unsigned)blocks, (unsigned)nb), dim3(k.threads), args, k.smem, st);
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
