@@ -17,6 +17,7 @@
 //     grad_x_j = Re sum_k g_k exp(+2 pi i jk/n)
 // over the bins Y exposes, which is C2R of g with interior bins halved
 // (half spectrum) or folded as (g_k + conj g_{n-k}) / 2 (full spectrum).
+#include <algorithm>
 #include <mutex>
 #include <set>
 
@@ -143,22 +144,22 @@ __global__ void __launch_bounds__(C2RCfg<T, LOGH, W>::THREADS)
 
 // pre-pass for sizes above the fused limit: Z' (H complex) into the output
 // buffer; pairs (k, H-k) per thread
+// (grid: x over the pairs of a transform, y over the batch, both strided)
 template <typename T, int W>
 __global__ void k_c2r_pre(const cpx<T> *in, cpx<T> *out, long long H, long long batch, long long idist,
                           long long odist, const cpx<T> *__restrict__ dtw)
 {
-    const long long pairs = H / 2 + 1;
-    for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < pairs * batch;
-         idx += (long long)gridDim.x * blockDim.x) {
-        const long long b = idx / pairs;
-        const int k = (int)(idx - b * pairs);
+    const int pairs = (int)(H / 2 + 1);
+    for (long long b = blockIdx.y; b < batch; b += gridDim.y) {
         const cpx<T> *f = in + b * idist;
         cpx<T> *z = out + b * odist;
         auto get = [f](int i) { return ld_c(f + i); };
-        const int p = (int)H - k;
-        const cpx<T> fk = c2r_bin<W, T>(get, k, (int)H), fp = c2r_bin<W, T>(get, p, (int)H);
-        st_c(z + k, c2r_pre_value(fk, fp, ldg_c(dtw + k)));
-        if (k > 0 && p != k) st_c(z + p, c2r_pre_value(fp, fk, ldg_c(dtw + p)));
+        for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < pairs; k += gridDim.x * blockDim.x) {
+            const int p = (int)H - k;
+            const cpx<T> fk = c2r_bin<W, T>(get, k, (int)H), fp = c2r_bin<W, T>(get, p, (int)H);
+            st_c(z + k, c2r_pre_value(fk, fp, ldg_c(dtw + k)));
+            if (k > 0 && p != k) st_c(z + p, c2r_pre_value(fp, fk, ldg_c(dtw + p)));
+        }
     }
 }
 
@@ -221,6 +222,15 @@ const C2REntry &c2r_entry(int dtype, int logh)
     return c2r_table<double>(std::make_integer_sequence<int, C2RMax<double>::value + 1>{})[logh];
 }
 
+// x over the pairs of a transform (256 a CTA), y over the batch; about 16K
+// CTAs at most, the kernels stride over the rest
+dim3 pair_grid(long long pairs, long long batch)
+{
+    const long long y = std::min<long long>(std::max<long long>(batch, 1), 65535);
+    const long long x = std::max<long long>(1, std::min<long long>((pairs + 255) / 256, std::max<long long>(1, 16384 / y)));
+    return dim3((unsigned)x, (unsigned)y);
+}
+
 unsigned grid_for2(long long work, int threads)
 {
     long long g = (work + threads - 1) / threads;
@@ -230,7 +240,7 @@ unsigned grid_for2(long long work, int threads)
 }
 
 template <typename T>
-void pre_launch(int w, unsigned g, const void *in, void *out, long long H, long long batch, long long idist,
+void pre_launch(int w, dim3 g, const void *in, void *out, long long H, long long batch, long long idist,
                 long long odist, const void *dtw, cudaStream_t st)
 {
     auto i = (const cpx<T> *)in;
@@ -270,7 +280,7 @@ cudaError_t launch_c2r_fused(int dtype, int logh, int wmode, const void *in, voi
 cudaError_t launch_c2r_pre(int dtype, int wmode, const void *in, void *out, long long H, long long batch,
                            long long idist, long long odist, const void *dtw, cudaStream_t st)
 {
-    const unsigned g = grid_for2((H / 2 + 1) * batch, 256);
+    const dim3 g = pair_grid(H / 2 + 1, batch);
     if (dtype == GFFT_F32) pre_launch<float>(wmode, g, in, out, H, batch, idist, odist, dtw, st);
     else pre_launch<double>(wmode, g, in, out, H, batch, idist, odist, dtw, st);
     return cudaGetLastError();

@@ -14,6 +14,7 @@
 // k_r2c_fused does all of it in one kernel (one HBM read of n reals, one
 // write of n/2+1 or n complex values) while n/2 fits one CTA; larger sizes
 // run the multi-pass C2C into the output buffer and then k_dit in place.
+#include <algorithm>
 #include <mutex>
 #include <set>
 
@@ -111,26 +112,27 @@ __global__ void __launch_bounds__(R2CCfg<T, LOGH>::THREADS)
 // Stand-alone adjustment (DIT<T>::apply, fft.h:180-188), in place or not:
 // thread p handles the pair (k, H - k), k = p in [0, H/2], reading both Z
 // values before writing, so out == in is safe.
+// (grid: x over the pairs of a transform, y over the batch, both strided)
 template <typename T, int MODE>
 __global__ void k_dit(const cpx<T> *in, cpx<T> *out, long long H, long long batch, long long idist,
                       long long odist, const cpx<T> *__restrict__ dtw, T scale)
 {
     const long long pairs = H / 2 + 1;
-    for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < pairs * batch;
-         idx += (long long)gridDim.x * blockDim.x) {
-        const long long b = idx / pairs;
-        const long long k = idx - b * pairs;
+    for (long long b = blockIdx.y; b < batch; b += gridDim.y) {
         const cpx<T> *z = in + b * idist;
         cpx<T> *f = out + b * odist;
-        const long long j = (H - k) & (H - 1);
-        const cpx<T> zk = ld_c(z + (k & (H - 1))), zj = ld_c(z + j);
-        const cpx<T> fk = scl(dit_value(zk, zj, ldg_c(dtw + k)), scale);
-        const cpx<T> fj = scl(dit_value(zj, zk, ldg_c(dtw + (H - k))), scale);
-        st_c(f + k, r2c_weight<MODE>(fk, k, H));
-        if (H - k != k) st_c(f + (H - k), r2c_weight<MODE>(fj, H - k, H));
-        if constexpr (MODE == R2C_FULL) {
-            if (k > 0) st_c(f + 2 * H - k, conj(fk));
-            if (k > 0 && H - k != k) st_c(f + H + k, conj(fj));
+        for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < pairs;
+             k += (long long)gridDim.x * blockDim.x) {
+            const long long j = (H - k) & (H - 1);
+            const cpx<T> zk = ld_c(z + (k & (H - 1))), zj = ld_c(z + j);
+            const cpx<T> fk = scl(dit_value(zk, zj, ldg_c(dtw + k)), scale);
+            const cpx<T> fj = scl(dit_value(zj, zk, ldg_c(dtw + (H - k))), scale);
+            st_c(f + k, r2c_weight<MODE>(fk, k, H));
+            if (H - k != k) st_c(f + (H - k), r2c_weight<MODE>(fj, H - k, H));
+            if constexpr (MODE == R2C_FULL) {
+                if (k > 0) st_c(f + 2 * H - k, conj(fk));
+                if (k > 0 && H - k != k) st_c(f + H + k, conj(fj));
+            }
         }
     }
 }
@@ -312,7 +314,7 @@ cudaError_t launch_r2c_fused(int dtype, int logh, int mode, const void *in, void
 }
 
 template <typename T>
-void dit_launch(int mode, unsigned g, const void *in, void *out, long long H, long long batch, long long idist,
+void dit_launch(int mode, dim3 g, const void *in, void *out, long long H, long long batch, long long idist,
                 long long odist, const void *dtw, cudaStream_t st, T sc)
 {
     auto i = (const cpx<T> *)in;
@@ -326,7 +328,11 @@ void dit_launch(int mode, unsigned g, const void *in, void *out, long long H, lo
 cudaError_t launch_dit(int dtype, int mode, const void *in, void *out, long long H, long long batch,
                        long long idist, long long odist, const void *dtw, cudaStream_t st, double scale)
 {
-    const unsigned g = grid_for((H / 2 + 1) * batch, 256);
+    // x over the pairs of a transform (256 a CTA), y over the batch; about
+    // 16K CTAs at most, the kernel strides over the rest
+    const long long gy = std::min<long long>(std::max<long long>(batch, 1), 65535);
+    const long long gx = std::max<long long>(1, std::min<long long>((H / 2 + 1 + 255) / 256, std::max<long long>(1, 16384 / gy)));
+    const dim3 g((unsigned)gx, (unsigned)gy);
     if (dtype == GFFT_F32) dit_launch<float>(mode, g, in, out, H, batch, idist, odist, dtw, st, (float)scale);
     else dit_launch<double>(mode, g, in, out, H, batch, idist, odist, dtw, st, scale);
     return cudaGetLastError();
