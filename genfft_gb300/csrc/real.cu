@@ -95,16 +95,25 @@ __global__ void __launch_bounds__(R2CCfg<T, LOGH>::THREADS)
     __syncthreads();
     if (!active) return;
     cpx<T> *dst = out + b * odist;
+    // pairs (k, H - k), k in [0, H/2]: both bins from the same two values
+    // (k = 0 gives bins 0 and H, k = H/2 is its own partner)
 #pragma unroll
-    for (int q = 0; q <= E; q++) {
-        const int k = t + q * G;  // k in [0, H] (q == E only reaches k == H)
-        if (k > H) break;
-        const int km = k & (H - 1);
+    for (int q = 0; q <= E / 2; q++) {
+        const int k = t + q * G;  // q == E/2 only reaches k == H/2
+        if (k > H / 2) break;
         const int j = (H - k) & (H - 1);
-        const cpx<T> f = scl(dit_value(my[spad<T>(km)], my[spad<T>(j)], ldg_c(dtw + k)), scale);
-        stcs_c(dst + k, r2c_weight<MODE>(f, k, H));
+        const cpx<T> zk = my[spad<T>(k)], zj = my[spad<T>(j)];
+        const cpx<T> fk = scl(dit_value(zk, zj, ldg_c(dtw + k)), scale);
+        stcs_c(dst + k, r2c_weight<MODE>(fk, k, H));
         if constexpr (MODE == R2C_FULL) {
-            if (k > 0 && k < H) stcs_c(dst + 2 * H - k, conj(f));
+            if (k > 0) stcs_c(dst + 2 * H - k, conj(fk));
+        }
+        if (H - k != k) {
+            const cpx<T> fj = scl(dit_value(zj, zk, ldg_c(dtw + (H - k))), scale);
+            stcs_c(dst + (H - k), r2c_weight<MODE>(fj, H - k, H));
+            if constexpr (MODE == R2C_FULL) {
+                if (k > 0) stcs_c(dst + H + k, conj(fj));
+            }
         }
     }
 }
