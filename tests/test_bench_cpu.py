@@ -70,3 +70,18 @@ def test_reference_arm_line(bench, monkeypatch):
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
     assert line["e2e"]["value"] == line["value"] and line["cpu_baseline"]["value"] > 0
     assert {"kind", "cores", "sample"} <= set(line["cpu_baseline"])
+
+
+def test_kernel_names_follow_the_paths(bench):
+    """`roofline.kernel` names the kernels each C2C size runs: fused up to
+    the fused limit, the persistent four-step (one launch), the three-pass
+    kernels (three launches a group, fp32 2^21 and up), else tile pairs."""
+    G = types.SimpleNamespace(F32=0, F64=1, max_fused_size=lambda d: (1 << 14) if d == 0 else (1 << 13))
+    K = bench.kernel_name
+    assert K(G, "c2c", "f32", 1 << 12) == "k_c2c_fused"
+    assert K(G, "c2c", "f32", 1 << 16, launches=1) == "k_fourstep"
+    assert K(G, "c2c", "f32", 1 << 22, launches=3).startswith("k3_col")
+    assert K(G, "c2c", "f32", 1 << 22, launches=6).startswith("k3_col")
+    assert K(G, "c2c", "f32", 1 << 20, launches=2) == "k_colpass_tma + k_rowpass_tma"
+    assert K(G, "c2c", "f64", 1 << 22, launches=2) == "k_colpass_tma + k_rowpass_tma"
+    assert K(G, "c2c", "f32", 1 << 16, mode=1) == "k_tc"
