@@ -36,7 +36,8 @@ def main() -> None:
     def cplx(shape, dt):
         return (rng.uniform(-1, 1, shape) + 1j * rng.uniform(-1, 1, shape)).astype(dt)
 
-    # 1D C2C, FFT<T>::transform<inv> (fft.h:80-85), n = 2^0 .. 2^12 (+2^14 f32)
+    # 1D C2C, FFT<T>::transform<inv> (fft.h:80-85), n = 2^0 .. 2^12 (+2^14 f32;
+    # more lengths at the end)
     for dt, tag in ((np.complex64, "f32"), (np.complex128, "f64")):
         sizes = list(range(0, 13)) + ([14] if tag == "f32" else [])
         for L in sizes:
@@ -150,6 +151,27 @@ def main() -> None:
         k = f"r2dlong_{tag}_{W}x{H}"
         data[k + "/in"] = x
         data[k + "/fwd_generic"] = gen.real_fft2d(x)
+
+    # Multi-pass and 32-points-a-thread lengths, appended last so the draws
+    # above are unchanged: C2C FFT<T>::transform<inv> (fft.h:80-85) at fp32
+    # 2^15 and fp64 2^13, 2^14 (the generic backend only, to keep the
+    # fixture small); RealFFT<float>::forward (FFTReal.h:204-213) at 2^14,
+    # 2^15
+    for L, dt, tag in ((15, np.complex64, "f32"), (13, np.complex128, "f64"), (14, np.complex128, "f64")):
+        n = 1 << L
+        x = cplx(n, dt)
+        k = f"c2c_{tag}_{n}"
+        data[k + "/in"] = x
+        data[k + "/fwd_generic"] = gen.fft(x, False)
+        data[k + "/inv_generic"] = gen.fft(x, True)
+    for L in (14, 15):
+        n = 1 << L
+        x = rng.uniform(-1, 1, n).astype(np.float32)
+        k = f"r2c_f32_{n}"
+        data[k + "/in"] = x
+        data[k + "/half_generic"] = gen.real_fft(x, True, fill=43 + 21j)
+        data[k + "/full_generic"] = gen.real_fft(x, False, fill=43 + 21j)
+        data[k + "/half_native"] = nat.real_fft(x, True, fill=43 + 21j)
 
     np.savez_compressed(OUT, **data)
     total = sum(v.nbytes for v in data.values())
