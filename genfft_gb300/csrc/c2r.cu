@@ -177,20 +177,6 @@ __global__ void k_c2r_one(const cpx<T> *in, T *out, long long batch, long long i
 
 namespace {
 
-cudaError_t smem_optin2(const void *fn, size_t smem)
-{
-    if (smem <= 48 * 1024) return cudaSuccess;
-    static std::mutex mu;
-    static std::set<std::pair<int, const void *>> done;
-    int dev = 0;
-    cudaGetDevice(&dev);
-    std::lock_guard<std::mutex> lk(mu);
-    if (done.count({dev, fn})) return cudaSuccess;
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e == cudaSuccess) done.insert({dev, fn});
-    return e;
-}
-
 struct C2REntry {
     const void *fn[3];
     int threads, tpc;
@@ -268,7 +254,7 @@ cudaError_t launch_c2r_fused(int dtype, int logh, int wmode, const void *in, voi
     const void *fn = e.fn[wmode];
     const size_t smem = e.smem[wmode];
     if (smem > C2R_SMEM_MAX) return cudaErrorInvalidValue;  // the planner routes these elsewhere
-    cudaError_t err = smem_optin2(fn, smem);
+    cudaError_t err = ensure_smem(fn, smem);
     if (err != cudaSuccess) return err;
     const long long grid = (batch + e.tpc - 1) / e.tpc;
     float scale_f = (float)scale;

@@ -39,6 +39,10 @@ void fused_twiddle_fill(int dtype, int logn, void *host_buf);  // writes that ma
 cudaError_t launch_fused_c2c(int dtype, int logn, int inverse, const FusedC2CArgs &a,
                              cudaStream_t st);
 
+// Opts fn in to `smem` bytes of dynamic shared memory when that is above
+// the 48 KB default, once per (device, function).
+cudaError_t ensure_smem(const void *fn, size_t smem);
+
 // Launches fn as a programmatic dependent of the previous kernel on the
 // stream: its CTAs may start while that kernel's last wave drains, and the
 // kernel (which begins with pdl_enter()) waits for that kernel's completion

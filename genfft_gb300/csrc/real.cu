@@ -225,20 +225,6 @@ __global__ void k_bitrev_swap(cpx<T> *x, int logn, long long batch, long long di
 
 namespace {
 
-cudaError_t smem_optin(const void *fn, size_t smem)
-{
-    if (smem <= 48 * 1024) return cudaSuccess;
-    static std::mutex mu;
-    static std::set<std::pair<int, const void *>> done;
-    int dev = 0;
-    cudaGetDevice(&dev);
-    std::lock_guard<std::mutex> lk(mu);
-    if (done.count({dev, fn})) return cudaSuccess;
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e == cudaSuccess) done.insert({dev, fn});
-    return e;
-}
-
 struct R2CEntry {
     const void *fn[3];
     int threads, tpc;
@@ -313,7 +299,7 @@ cudaError_t launch_r2c_fused(int dtype, int logh, int mode, const void *in, void
 {
     const R2CEntry &e = r2c_entry(dtype, logh);
     const void *fn = e.fn[mode];
-    cudaError_t err = smem_optin(fn, e.smem);
+    cudaError_t err = ensure_smem(fn, e.smem);
     if (err != cudaSuccess) return err;
     const long long grid = (batch + e.tpc - 1) / e.tpc;
     float scale_f = (float)scale;

@@ -205,20 +205,6 @@ TpReg<7, 8, 8, 32, 16, 16> tp23;
 TpReg<8, 7, 8, 16, 32, 16> tp23_1;
 TpReg<8, 8, 8, 16, 16, 16> tp24;
 
-cudaError_t opt_in(const void *fn, size_t smem)
-{
-    if (smem <= 48 * 1024) return cudaSuccess;
-    static std::mutex mu;
-    static std::map<std::pair<int, const void *>, bool> done;
-    int dev = 0;
-    cudaGetDevice(&dev);
-    std::lock_guard<std::mutex> lk(mu);
-    if (done.count({dev, fn})) return cudaSuccess;
-    const cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e == cudaSuccess) done[{dev, fn}] = true;
-    return e;
-}
-
 }  // namespace
 
 const ThreePass *threepass_find(int dtype, int logn)
@@ -240,7 +226,7 @@ cudaError_t launch_threepass(const ThreePass &k, int inverse, const ThreePassArg
     const long long A = 1LL << k.la, B = 1LL << k.lb, C = 1LL << k.lc, M = B * C, N = A * M;
     const void *const *fn = inverse ? k.inv : k.fwd;
     for (int p = 0; p < 3; p++) {
-        const cudaError_t e = opt_in(fn[p], k.smem[p]);
+        const cudaError_t e = ensure_smem(fn[p], k.smem[p]);
         if (e != cudaSuccess) return e;
     }
     const unsigned nmask1 = (unsigned)(N - 1), nmask2 = (unsigned)(M - 1);

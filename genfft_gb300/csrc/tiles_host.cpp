@@ -26,20 +26,6 @@ std::mutex &reg_mu()
     return m;
 }
 
-// large dynamic shared memory needs an opt-in per (device, function)
-cudaError_t ensure_smem(const void *fn, size_t smem)
-{
-    if (smem <= 48 * 1024) return cudaSuccess;
-    static std::mutex mu;
-    static std::set<std::pair<int, const void *>> done;
-    int dev = 0;
-    cudaGetDevice(&dev);
-    std::lock_guard<std::mutex> lk(mu);
-    if (done.count({dev, fn})) return cudaSuccess;
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e == cudaSuccess) done.insert({dev, fn});
-    return e;
-}
 int sm_count()
 {
     static std::mutex mu;
@@ -56,6 +42,20 @@ int sm_count()
 }
 
 }  // namespace
+
+cudaError_t ensure_smem(const void *fn, size_t smem)
+{
+    if (smem <= 48 * 1024) return cudaSuccess;
+    static std::mutex mu;
+    static std::set<std::pair<int, const void *>> done;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(mu);
+    if (done.count({dev, fn})) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) done.insert({dev, fn});
+    return e;
+}
 
 cudaError_t launch_pdl(const void *fn, dim3 grid, dim3 block, void **args, size_t smem, cudaStream_t st)
 {
