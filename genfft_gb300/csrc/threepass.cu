@@ -190,13 +190,18 @@ struct TpReg {
 // (a, b, c, pass-1 columns, pass-2 columns, pass-3 rows): tiles of 2048 -
 // 4096 points, runs of 16 - 64 points.  The first layout of a length is
 // the default, the others are selected by GFFT_3PASS_VARIANT.  Measured on
-// GB300 (GB/s, 1 GB batches, forward + inverse):
+// GB300 (GB/s, 1 GB batches, forward + inverse; 2^19 and 2^20 run two
+// passes by default, 2029 and 2136):
+//   2^19  (6,6,7 | 64,64,16) 2085   (6,7,6 | 64,32,32) 1886, (5,7,7) 1652
+//   2^20  (6,6,8 | 64,64,16) 2102   (7,6,7 | 32,64,16) 2065, (6,7,7) 2056
 //   2^21  (7,7,7 | 32,32,16) 2118   (7,6,8 | 32,64,16) 2057
 //   2^22  (7,7,8 | 32,32,16) 2095   (7,8,7 | 32,16,16) 2040, four other
 //         shapes 1951-2044
 //   2^23  (7,8,8 | 32,16,16) 2017   (8,7,8 | 16,32,16) 1978
-TpReg<6, 7, 6, 64, 32, 32> tp19;
-TpReg<7, 6, 7, 32, 64, 16> tp20;
+TpReg<6, 6, 7, 64, 64, 16> tp19;
+TpReg<6, 7, 6, 64, 32, 32> tp19_1;
+TpReg<6, 6, 8, 64, 64, 16> tp20;
+TpReg<7, 6, 7, 32, 64, 16> tp20_1;
 TpReg<7, 7, 7, 32, 32, 16> tp21;
 TpReg<7, 6, 8, 32, 64, 16> tp21_1;
 TpReg<7, 7, 8, 32, 32, 16> tp22;
