@@ -18,8 +18,6 @@
 // over the bins Y exposes, which is C2R of g with interior bins halved
 // (half spectrum) or folded as (g_k + conj g_{n-k}) / 2 (full spectrum).
 #include <algorithm>
-#include <mutex>
-#include <set>
 
 #include "internal.h"
 #include "plan.h"

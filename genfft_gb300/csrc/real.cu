@@ -15,8 +15,6 @@
 // write of n/2+1 or n complex values) while n/2 fits one CTA; larger sizes
 // run the multi-pass C2C into the output buffer and then k_dit in place.
 #include <algorithm>
-#include <mutex>
-#include <set>
 
 #include "internal.h"
 #include "plan.h"

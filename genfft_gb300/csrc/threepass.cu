@@ -20,7 +20,6 @@
 #include <cstdlib>
 #include <map>
 #include <mutex>
-#include <utility>
 #include <vector>
 
 #include "internal.h"
